@@ -1,0 +1,426 @@
+"""Benchmark of the GB300 simus/pfield sweep.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload (one "step" = one frame): the 128-element scale configuration -- 200,000 scatterers
+in x in [-19, 19] mm, z in [5, 50] mm with three anechoic disks, 0.5 dB/cm/MHz, one 0-degree
+plane wave -> 128-channel RF (plain fused FP32 simus sweep + cuFFT irfft + gate), plus the RMS
+pressure field on a 256 x 512 grid over the same box.  Inputs are seeded synthetic data.
+
+The JSON line reports RF frames/s (``value``, inputs resident in HBM, L2 flushed before every
+step), the same through the public API with host buffers (``e2e``), Green's terms/s, the FP32
+roofline of the dominant kernel, the CPU baseline (the oracle: a port of the reference's FP64
+NumPy path, timed on this host's cores on a bounded sample and scaled per scatterer/point),
+and SM clocks sampled during the timed region.
+
+``--impl reference`` times that CPU path alone, each step a bounded sample, and prints the
+same metric with ``"impl": "reference"``.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "RF frames/s (plain fused FP32 simus sweep + 256x512 pfield per frame)"
+UNIT = "frames/s"
+WORKLOAD = ("cfg2: 128-element linear array (pitch 0.30 mm, width 0.27 mm, fc 5.2 MHz, bw 0.67), "
+            "c 1540 m/s, 0.5 dB/cm/MHz, 0-degree plane wave, 200,000 scatterers x in [-19,19] mm, "
+            "z in [5,50] mm, rc N(0,1) with three 2 mm anechoic disks; + pfield on 256x512 grid")
+L2_FLUSH_BYTES = 512 << 20
+
+
+def _env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def _cpu_info():
+    model = "unknown"
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu model")):
+                model = line.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
+    if model == "unknown":
+        try:
+            out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+            for line in out.splitlines():
+                if "Model name" in line:
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except Exception:
+            pass
+    return model, len(os.sched_getaffinity(0))
+
+
+# ------------------------------------------------------------------------------------------
+# CPU baseline: the oracle (FP64 NumPy port of the reference's PYTHON strategy)
+# ------------------------------------------------------------------------------------------
+
+def _oracle_simus_shard(args):
+    import oracle.fastsimus_fp64 as O
+
+    scat, rc, delays, plan, params, medium = args
+    return O.simus_spectrum_selected(scat, rc, delays, plan, params, medium)
+
+
+def _oracle_pfield_shard(args):
+    import oracle.fastsimus_fp64 as O
+
+    pts, delays, plan, params, medium = args
+    return O.pfield_compute(pts, delays, plan, params, medium)
+
+
+def cpu_frame_time(pool, n_workers, scat, rc, grid_pts, delays, plan, pplan, params, medium, s_sample, g_sample):
+    """Seconds per full frame, extrapolated linearly from a sample of s_sample scatterers and
+    g_sample grid points (the sweep cost is linear in both; plan and irfft are excluded on
+    both arms)."""
+    import oracle.fastsimus_fp64 as O
+
+    rng = np.random.default_rng(123)
+    si = rng.choice(scat.shape[0], s_sample, replace=False)
+    gi = rng.choice(grid_pts.shape[0], g_sample, replace=False)
+    s_sh = np.array_split(si, n_workers)
+    g_sh = np.array_split(gi, n_workers)
+    t0 = time.perf_counter()
+    parts = pool.map(_oracle_simus_shard, [(scat[i], rc[i], delays, plan, params, medium) for i in s_sh])
+    spec = sum(parts) * plan.correction_factor
+    O.irfft_and_threshold(spec, plan, params.n_elements)
+    t1 = time.perf_counter()
+    pool.map(_oracle_pfield_shard, [(grid_pts[i], delays, pplan, params, medium) for i in g_sh])
+    t2 = time.perf_counter()
+    return (t1 - t0) * scat.shape[0] / s_sample + (t2 - t1) * grid_pts.shape[0] / g_sample
+
+
+def make_workload():
+    from fastsimus_gb300 import workloads as W
+    from fastsimus_gb300.plan import pfield_precompute, simus_precompute
+
+    params, medium = W.cfg2_probe(), W.cfg2_medium()
+    scat, rc = W.cfg2_scatterers()
+    grid = W.cfg2_grid()
+    delays = np.zeros(params.n_elements)
+    t0 = time.perf_counter()
+    plan = simus_precompute(scat, rc, delays, params, medium)
+    pplan = pfield_precompute(grid, delays, params, medium)
+    t_plan = time.perf_counter() - t0
+    return params, medium, scat, rc, grid, delays, plan, pplan, t_plan
+
+
+def green_terms(plan, pplan, params, n_scat, n_grid):
+    e_u = params.n_elements * plan.n_sub
+    return n_scat * e_u * plan.selected_freqs.shape[0] + n_grid * e_u * pplan.selected_freqs.shape[0]
+
+
+def algorithmic_flops_simus(plan, params, n_scat, n_tx=1):
+    """S * F * (8 E U + 16 E T): recurrence (6) + sub-sum (2) per term, TX and RX complex MAC
+    (8 + 8) per (scatterer, element, frequency, transmit)."""
+    E, U, F = params.n_elements, plan.n_sub, plan.selected_freqs.shape[0]
+    return float(n_scat) * F * (8.0 * E * U + 16.0 * E * n_tx)
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        print(json.dumps({"impl": "reference", "rank": rank, "skipped": "rank 0 runs the CPU arm"}), file=sys.stderr)
+        return
+    import multiprocessing as mp
+
+    params, medium, scat, rc, grid, delays, plan, pplan, _ = make_workload()
+    gpts = grid.reshape(-1, 2)
+    model, cores = _cpu_info()
+    ctx = mp.get_context("spawn")
+    s_sample, g_sample = args.cpu_scatterers, args.cpu_points
+    with ctx.Pool(cores) as pool:
+        for _ in range(max(args.warmup, 0)):
+            cpu_frame_time(pool, cores, scat, rc, gpts, delays, plan, pplan, params, medium, max(cores, 64),
+                           max(cores, 64))
+        times = [cpu_frame_time(pool, cores, scat, rc, gpts, delays, plan, pplan, params, medium, s_sample,
+                                g_sample) for _ in range(args.steps)]
+    t = float(np.mean(times))
+    val = 1.0 / t
+    sample = (f"{s_sample} of {scat.shape[0]} scatterers and {g_sample} of {gpts.shape[0]} grid points per step, "
+              f"sharded over {cores} processes, time scaled linearly to the full frame")
+    line = {
+        "metric": METRIC, "value": val, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "cpu": model, "l2": "n/a (CPU)"},
+        "green_terms_per_s": green_terms(plan, pplan, params, scat.shape[0], gpts.shape[0]) * val,
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------------
+
+class ClockSampler:
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            pass
+    return {}
+
+
+def fp32_peak_tflops(device):
+    """Measured FP32 FMA throughput (TFLOP/s) of this GPU from fsg_fp32_fma_probe."""
+    import ctypes
+
+    import torch
+
+    from fastsimus_gb300 import _native
+
+    lib = _native.load()
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    blocks = sms * 8
+    out = torch.empty(blocks, dtype=torch.float32, device=device)
+    flops = ctypes.c_double()
+    stream = torch.cuda.current_stream(device).cuda_stream
+    best = 0.0
+    for it in range(4):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        _native.check(lib.fsg_fp32_fma_probe(out.data_ptr(), blocks, 1 << 16, ctypes.byref(flops), stream))
+        e.record()
+        torch.cuda.synchronize()
+        if it:
+            best = max(best, flops.value / (s.elapsed_time(e) * 1e-3) / 1e12)
+    return best
+
+
+def run_gpu_arm(args, rank, world):
+    import torch
+
+    import fastsimus_gb300 as F
+    from fastsimus_gb300 import _device, build
+
+    build.build()
+    local = _env_int("LOCAL_RANK", 0)
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=device)
+
+    params, medium, scat, rc, grid, delays, plan, pplan, t_plan = make_workload()
+    n_scat, n_grid = scat.shape[0], grid.shape[0] * grid.shape[1]
+
+    # device-resident inputs
+    scat_d = torch.as_tensor(scat, device=device)
+    rc_d = torch.as_tensor(rc, device=device)
+    grid_d = torch.as_tensor(grid, device=device)
+    del_d = torch.as_tensor(delays, device=device)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
+
+    def step_device():
+        res = F.simus_compute(scat_d, rc_d, del_d, plan, params, medium)
+        pf = F.pfield_compute(grid_d, del_d, pplan, params, medium)
+        return res, pf
+
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+
+    timer = _device.LaunchTimer()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        _device.set_timer(timer)
+        for k in range(args.steps):
+            flush.zero_()
+            starts[k].record()
+            step_device()
+            ends[k].record()
+        torch.cuda.synchronize()
+        _device.set_timer(None)
+    dev_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    if dist is not None:
+        t = torch.tensor([dev_ms], device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_ms = float(t.item())
+        dist.barrier()
+    frames = args.steps * world
+    value = frames / (dev_ms * 1e-3)
+    simus_ms = timer.elapsed_ms("fsg_simus")
+    pfield_ms = timer.elapsed_ms("fsg_pfield")
+
+    # end-to-end through the public API with host (pinned) buffers
+    scat_h = torch.as_tensor(scat).pin_memory()
+    rc_h = torch.as_tensor(rc).pin_memory()
+    grid_h = torch.as_tensor(grid).pin_memory()
+    del_h = torch.as_tensor(delays).pin_memory()
+    res, pf = step_device()
+    rf_out = torch.empty(res.rf.shape, dtype=res.rf.dtype).pin_memory()
+    pf_out = torch.empty(pf.shape, dtype=pf.dtype).pin_memory()
+    h2d = sum(t.numel() * t.element_size() for t in (scat_h, rc_h, grid_h, del_h))
+    d2h = rf_out.numel() * rf_out.element_size() + pf_out.numel() * pf_out.element_size()
+    e2e_ms = []
+    for k in range(args.warmup + args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        r = F.simus_compute(scat_h, rc_h, del_h, plan, params, medium)
+        p = F.pfield_compute(grid_h, del_h, pplan, params, medium)
+        rf_out.copy_(r.rf, non_blocking=True)
+        pf_out.copy_(p, non_blocking=True)
+        e.record()
+        torch.cuda.synchronize()
+        if k >= args.warmup:
+            e2e_ms.append(s.elapsed_time(e))
+    e2e_total = sum(e2e_ms)
+    if dist is not None:
+        t = torch.tensor([e2e_total], device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e_value = frames / (e2e_total * 1e-3)
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    peak = fp32_peak_tflops(device)
+    flops = algorithmic_flops_simus(plan, params, n_scat)
+    simus_avg = float(np.mean(simus_ms)) if simus_ms else float("nan")
+    achieved = flops / (simus_avg * 1e-3) / 1e12
+    gt = green_terms(plan, pplan, params, n_scat, n_grid)
+    peaks = _peaks()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (double-float phase)", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "parallelism": "replicas" if world > 1 else "1 gpu",
+                   "l2": f"flushed before every timed step ({L2_FLUSH_BYTES >> 20} MiB write)",
+                   "n_freq_simus": int(plan.selected_freqs.shape[0]), "n_freq_pfield": int(pplan.selected_freqs.shape[0]),
+                   "n_sub": int(plan.n_sub), "plan_host_s": t_plan},
+        "green_terms_per_s": gt * value,
+        "simus_ms": simus_avg, "pfield_ms": float(np.mean(pfield_ms)) if pfield_ms else None,
+        "gpu_launches": 6 * args.steps,
+        "roofline": {"kernel": "simus_band_kernel", "bound": "fp32", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak if peak else None, "traffic": None,
+                     "peak_source": "measured in-run by fsg_fp32_fma_probe (FP32 FMA chains); MEASURED_PEAKS.json "
+                                    "holds only HBM and bf16 tensor peaks",
+                     "algorithmic_flops_per_launch": flops,
+                     "hbm_peak_gbs": peaks.get("hbm_gbs")},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "clocks": clocks.summary(),
+    }
+    if not args.no_cpu_baseline:
+        import multiprocessing as mp
+
+        model, cores = _cpu_info()
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(cores) as pool:
+            cpu_frame_time(pool, cores, scat, rc, grid.reshape(-1, 2), delays, plan, pplan, params, medium,
+                           cores, cores)
+            t = cpu_frame_time(pool, cores, scat, rc, grid.reshape(-1, 2), delays, plan, pplan, params, medium,
+                               args.cpu_scatterers, args.cpu_points)
+        line["cpu_baseline"] = {
+            "value": 1.0 / t, "unit": UNIT, "cores": cores, "kind": "port", "cpu": model,
+            "sample": f"{args.cpu_scatterers} scatterers + {args.cpu_points} grid points of the frame, sharded over "
+                      f"{cores} processes, scaled linearly to 200,000 scatterers + 131,072 points"}
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--cpu-scatterers", type=int, default=2048)
+    ap.add_argument("--cpu-points", type=int, default=4096)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1)
+    if args.impl == "reference":
+        run_reference_arm(args, rank, world)
+    else:
+        run_gpu_arm(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

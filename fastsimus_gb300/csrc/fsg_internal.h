@@ -1,0 +1,92 @@
+// Internal declarations shared by the sweep kernels (fsg_sweep.cu) and the C ABI (fsg_api.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "fsg_common.cuh"
+
+namespace fsg {
+
+struct Tables {
+  float4* src_pos;   // [n_src] x_hi, x_lo, z_hi, z_lo
+  float* theta_e;    // [E]
+  float2* kf;        // [F] k_f double-float
+  float* af;         // [F] attenuation Np/m at f
+  float2* pp;        // [F] pulse * probe
+  float* probe;      // [F]
+  float2* da;        // [n_anchor][E] apod * exp(i 2 pi f_anchor tau)
+  float2* dstep;     // [E] exp(i 2 pi df tau)
+};
+
+struct SetupArgs {
+  int E, U, F, n_anchor;
+  double pitch, width, radius, c, att, f0, df, seg;
+  const double* delays;
+  const double* apod;
+  const double* pulse;  // F complex128
+  const double* probe;  // F float64
+  Tables t;
+};
+
+struct BandArgs {
+  const double* pts;   // [n_pts*2]
+  const double* rc;    // [n_pts] (simus) or NULL (pfield)
+  int64_t n_pts;
+  int64_t per_slice;   // points per slice (multiple of st)
+  Tables t;
+  SweepConst C;
+  int E, U, n_src, gn, st, fb, F, n_anchor;
+  int convex;
+  double apex, radius2;
+  void* partial;       // simus: float2 [slices][F][E]; pfield: float [bands][n_pts]
+};
+
+struct SmemLayout {
+  int rows, pitch;     // geometry rows (gn * kSrcPerThread) and row pitch (st + 1)
+  size_t off_rhi, off_rlo, off_amp, off_step, off_w, off_pp, off_ka, off_aa, off_da, total;
+};
+
+__host__ __device__ inline size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
+
+__host__ __device__ inline SmemLayout smem_layout(int gn, int st, int fb, int E, bool with_w) {
+  SmemLayout L;
+  L.rows = gn * kSrcPerThread;
+  L.pitch = st + 1;
+  size_t n = (size_t)L.rows * L.pitch;
+  size_t o = 0;
+  L.off_rhi = o; o = align16(o + n * 4);
+  L.off_rlo = o; o = align16(o + n * 4);
+  L.off_amp = o; o = align16(o + n * 4);
+  L.off_step = o; o = align16(o + n * 8);
+  L.off_w = o; o = align16(o + (with_w ? (size_t)fb * st * 8 : 0));
+  L.off_pp = o; o = align16(o + (size_t)fb * 8);
+  int na = fb / kAnchor;
+  L.off_ka = o; o = align16(o + (size_t)na * 8);
+  L.off_aa = o; o = align16(o + (size_t)na * 4);
+  L.off_da = o; o = align16(o + (size_t)na * E * 8);
+  L.total = o;
+  return L;
+}
+
+struct SweepConfig {
+  int gn, st, fb, n_bands, n_slices;
+  int64_t per_slice;
+  size_t smem;
+};
+
+__global__ void setup_tables(SetupArgs a);
+// Launches simus_band_kernel<U> (U = n_sub in 1..4) with c's grid and shared memory.
+cudaError_t launch_simus_band_any(int U, const SweepConfig& c, const BandArgs& A, cudaStream_t s);
+__global__ void pfield_band_kernel(const BandArgs A);
+__global__ void simus_reduce(const float2* __restrict__ partial, int n_slices, int F, int E,
+                             const float* __restrict__ probe, float corr, int full, int n_rows, int idx0,
+                             float2* __restrict__ out);
+__global__ void pfield_reduce(const float* __restrict__ partial, int n_bands, int64_t n_pts, float corr,
+                              float* __restrict__ out);
+
+int set_error(int code, const char* fmt, ...);
+int check_cuda(cudaError_t err, const char* what);
+
+}  // namespace fsg

@@ -1,0 +1,144 @@
+/*
+ * fsgb300.h -- C ABI of libfsgb300.so, the GB300 (sm_103a) implementation of the
+ * FastSIMUS simus/pfield frequency sweep.
+ *
+ * Conventions
+ *   - Every array argument is a DEVICE pointer unless stated otherwise; sizes are element
+ *     counts.  Complex values are interleaved (re, im).
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).  Calls are
+ *     asynchronous on that stream; the caller synchronises.
+ *   - The library allocates no device memory: the caller passes a workspace of at least the
+ *     size reported by the matching *_workspace_size() function.
+ *   - Every entry point returns an FsgStatus; fsg_last_error_string() gives a one-line
+ *     message for the calling thread's last failure.
+ *   - NaN transmit delays are treated as (delay 0, apodization 0), as the reference's
+ *     simus_compute/pfield_compute do before their sweep (simus.py:427-429, pfield.py:338-340).
+ */
+#ifndef FSGB300_H
+#define FSGB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FSG_ABI_VERSION 1
+
+typedef enum FsgStatus {
+  FSG_OK = 0,
+  FSG_EINVAL = 1,        /* bad argument (NULL pointer, size out of range, ...) */
+  FSG_ECUDA = 2,         /* a CUDA runtime call failed */
+  FSG_ETIMEOUT = 3,      /* a bounded device-side wait gave up */
+  FSG_EUNSUPPORTED = 4,  /* valid request this build does not implement */
+  FSG_EWORKSPACE = 5     /* workspace smaller than *_workspace_size() */
+} FsgStatus;
+
+typedef enum FsgBaffle {
+  FSG_BAFFLE_SOFT = 0,      /* obliquity cos(theta) */
+  FSG_BAFFLE_RIGID = 1,     /* obliquity 1 */
+  FSG_BAFFLE_IMPEDANCE = 2  /* obliquity cos(theta) / (cos(theta) + baffle_impedance) */
+} FsgBaffle;
+
+typedef enum FsgOutLayout {
+  /* (F, E) complex64: selected-band spectrum before the correction factor, the return
+   * contract of the reference's simus_cuda (kernels/cuda_simus.py:232-321). */
+  FSG_OUT_SELECTED_RAW = 0,
+  /* (n_freq_full, E) complex64: selected band times correction_factor placed at rows
+   * [freq_idx_start, freq_idx_start + F), zeros elsewhere -- the array the reference's
+   * _irfft_and_threshold builds before its irfft (simus.py:336-352). */
+  FSG_OUT_FULL_CORRECTED = 1
+} FsgOutLayout;
+
+/* Transducer array: the fields of TransducerParams (transducer_params.py:23-160) that the
+ * sweep reads.  radius = +INFINITY for a linear array. */
+typedef struct FsgProbe {
+  int32_t n_elements;
+  int32_t n_sub;            /* sub-elements per element (plan.n_sub) */
+  double pitch;
+  double element_width;
+  double radius;
+  double freq_center;
+  int32_t baffle;           /* FsgBaffle */
+  int32_t reserved0;
+  double baffle_impedance;  /* used when baffle == FSG_BAFFLE_IMPEDANCE */
+} FsgProbe;
+
+/* MediumParams (medium_params.py:6-22). attenuation in dB/cm/MHz. */
+typedef struct FsgMedium {
+  double speed_of_sound;
+  double attenuation;
+} FsgMedium;
+
+/* Frequency plan (SimusPlan / PfieldPlan, simus.py:135-162, pfield.py:58-82).
+ * The sweep advances from freq_start by freq_step = selected_freqs[1] - selected_freqs[0],
+ * as the reference's recurrence does (simus.py:302-308). */
+typedef struct FsgFreqPlan {
+  int32_t n_freq;                 /* F, number of selected frequencies */
+  int32_t n_freq_full;            /* simus only: rows of the full spectrum */
+  int32_t freq_idx_start;         /* simus only: row of the first selected frequency */
+  int32_t reserved0;
+  double freq_start;              /* selected_freqs[0], Hz */
+  double freq_step;               /* selected_freqs[1] - selected_freqs[0], Hz (0 if F == 1) */
+  double seg_length;              /* element_width / n_sub */
+  double correction_factor;       /* df * element_width */
+  const double* pulse_spectrum;   /* device, F complex128 (interleaved) */
+  const double* probe_spectrum;   /* device, F float64 */
+} FsgFreqPlan;
+
+/* ABI version compiled into the library (FSG_ABI_VERSION). */
+int32_t fsg_abi_version(void);
+
+/* Message describing the calling thread's most recent failure ("" if none). */
+const char* fsg_last_error_string(void);
+
+/* Workspace bytes needed by fsg_simus for this probe / plan / scatterer count. */
+size_t fsg_simus_workspace_size(const FsgProbe* probe, const FsgFreqPlan* plan, int64_t n_scat);
+
+/*
+ * Plain fused FP32 simus sweep for one transmit.
+ * Replaces simus_cuda(scatterers, rc, params, plan, medium, delays_clean, tx_apodization)
+ * (kernels/cuda_simus.py:232-321, launched from simus.py:455-469) and the PYTHON-strategy
+ * sweep it stands in for (_simus_strategies.py:23-149).
+ *
+ *   scat_xz [n_scat*2] float64   scatterer (x, z) in metres, interleaved
+ *   rc      [n_scat]   float64   reflection coefficients
+ *   delays  [E]        float64   transmit delays in seconds (NaN = element off)
+ *   apod    [E]        float64   transmit apodization (NULL = all ones)
+ *   out     complex64, layout per out_layout (FsgOutLayout)
+ * full_frequency_directivity != 0 evaluates the element directivity at every frequency
+ * (_simus_strategies.py:59-62) instead of at the centre frequency only.
+ */
+int32_t fsg_simus(const FsgProbe* probe, const FsgMedium* medium, const FsgFreqPlan* plan,
+                  const double* scat_xz, const double* rc, int64_t n_scat,
+                  const double* delays, const double* apod,
+                  int32_t full_frequency_directivity, int32_t out_layout, void* out,
+                  void* workspace, size_t workspace_bytes, void* stream);
+
+/* Workspace bytes needed by fsg_pfield for this probe / plan / point count. */
+size_t fsg_pfield_workspace_size(const FsgProbe* probe, const FsgFreqPlan* plan, int64_t n_points);
+
+/*
+ * RMS pressure field sqrt(correction * sum_f |pulse*probe * sum_src G|^2) at n_points points.
+ * Replaces pfield_metal (kernels/metal_pfield.py:89-115) plus the final sqrt of
+ * pfield_compute (pfield.py:374-378); the sweep it computes is _pfield_strategies.py:21-88.
+ *   points  [n_points*2] float64 (x, z) interleaved
+ *   out     [n_points]   float32 RMS pressure
+ */
+int32_t fsg_pfield(const FsgProbe* probe, const FsgMedium* medium, const FsgFreqPlan* plan,
+                   const double* points, int64_t n_points, const double* delays, const double* apod,
+                   int32_t full_frequency_directivity, float* out,
+                   void* workspace, size_t workspace_bytes, void* stream);
+
+/* Measurement utility, no counterpart in the reference: launches `blocks` x 256 threads of
+ * independent FP32 FMA chains (`iters` iterations) and reports the FLOPs it performs, so a
+ * caller can time it with events and state the device's FP32 FMA roofline.  `out` must hold
+ * `blocks` floats (written only in a case that does not occur). */
+int32_t fsg_fp32_fma_probe(float* out, int32_t blocks, int32_t iters, double* flops, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FSGB300_H */

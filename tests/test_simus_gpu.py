@@ -1,0 +1,148 @@
+"""GPU parity of the plain fused FP32 simus kernel (through the C ABI) against the reference's
+golden vectors and the CPU oracle.  Tolerance: relative L2 <= 1e-5 on RF and on the
+selected-band spectrum (the plain-kernel target); max phase error reported."""
+
+import numpy as np
+import pytest
+
+import oracle.fastsimus_fp64 as O
+from tests import _golden as G
+from tests._gpu import np64, require_gpu, torch
+
+pytestmark = pytest.mark.gpu
+
+PLAIN_TOL = 1e-5
+CASES = [n for n in G.names("simus_") if not n.startswith("simus_multi") and "ffd" not in n]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _gpu():
+    require_gpu()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_simus_rf_matches_reference_golden(name):
+    import fastsimus_gb300 as F
+
+    g = G.load(name)
+    res = F.simus(g.scatterers, g.rc, g.delays, g.params, g.medium, fs=g.fs, tx_apodization=g.apod,
+                  element_splitting=g.element_splitting)
+    rf = np64(res.rf)
+    assert rf.shape == g.rf.shape
+    err = G.rel_l2(rf, g.rf)
+    print(f"{name}: rf relL2 = {err:.3e}")
+    assert err < PLAIN_TOL
+    if hasattr(g, "spectrum_selected"):
+        i0 = int(g.plan_freq_idx_start)
+        sel = np64(res.spectrum)[i0: i0 + g.plan_selected_freqs.shape[0]]
+        e2 = G.rel_l2(sel, g.spectrum_selected)
+        ph = G.max_phase_err(sel, g.spectrum_selected)
+        print(f"{name}: spectrum relL2 = {e2:.3e}, max phase err = {ph:.3e} rad")
+        assert e2 < PLAIN_TOL
+
+
+def test_hook_selected_raw_matches_oracle():
+    """simus_gb300 (the simus_cuda-shaped hook) returns the pre-correction selected band."""
+    import fastsimus_gb300 as F
+
+    g = G.load("simus_small_nan_apod")
+    plan = F.simus_precompute(g.scatterers, g.rc, g.delays, g.params, g.medium)
+    d = np.where(np.isnan(g.delays), 0.0, g.delays)
+    a = np.where(np.isnan(g.delays), 0.0, g.apod)
+    out = np64(F.simus_gb300(g.scatterers, g.rc, g.params, plan, g.medium, d, a))
+    ref = O.simus_spectrum_selected(g.scatterers, g.rc, d, plan, g.params, g.medium, tx_apodization=a)
+    assert out.shape == ref.shape
+    assert G.rel_l2(out, ref) < PLAIN_TOL
+
+
+def test_multi_transmit_shared_plan_matches_reference():
+    import fastsimus_gb300 as F
+
+    g = G.load("simus_multi3_cfg1")
+    plan = F.simus_precompute(g.scatterers, g.rc, g.delays[int(g.plan_source)], g.params, g.medium)
+    rf = np.stack([np64(F.simus_compute(g.scatterers, g.rc, d, plan, g.params, g.medium).rf) for d in g.delays], -1)
+    assert G.rel_l2(rf, g.rf) < PLAIN_TOL
+
+
+def test_zero_scatterers_and_zero_rc_give_zero_rf():
+    import fastsimus_gb300 as F
+    from fastsimus_gb300 import workloads as W
+
+    p, m = W.cfg1_probe(), W.cfg1_medium()
+    s, r = W.cfg1_scatterers(50)
+    plan = F.simus_precompute(s, r, np.zeros(64), p, m)
+    res0 = F.simus_compute(np.zeros((0, 2)), np.zeros(0), np.zeros(64), plan, p, m)
+    assert float(res0.rf.abs().max()) == 0.0
+    res1 = F.simus_compute(s, np.zeros(50), np.zeros(64), plan, p, m)
+    assert float(res1.rf.abs().max()) < 1e-10
+
+
+def test_single_scatterer_and_out_of_field():
+    import fastsimus_gb300 as F
+    from fastsimus_gb300.params import P4_2v
+
+    p = P4_2v()
+    s = np.array([[0.0, 3e-2]])
+    res = F.simus(s, np.ones(1), np.zeros(64), p)
+    rf = np64(res.rf)
+    ref = O.simus(s, np.ones(1), np.zeros(64), p, F.MediumParams())
+    assert np.abs(rf).max() > 0
+    assert G.rel_l2(rf, ref.rf) < PLAIN_TOL
+    # a scatterer behind the array (z < 0) contributes nothing
+    res2 = F.simus(np.array([[0.0, 3e-2], [0.0, -1e-2]]), np.ones(2), np.zeros(64), p)
+    plan = F.simus_precompute(np.array([[0.0, 3e-2], [0.0, -1e-2]]), np.ones(2), np.zeros(64), p)
+    res3 = F.simus_compute(s, np.ones(1), np.zeros(64), plan, p)
+    assert G.rel_l2(np64(res2.spectrum), np64(res3.spectrum)) < 1e-6
+
+
+def test_linearity_in_scatterers_at_scale():
+    """Spectrum is linear in the scatterer set: S(A u B) = S(A) + S(B) (size-independent
+    property used at full scale)."""
+    import fastsimus_gb300 as F
+    from fastsimus_gb300 import workloads as W
+
+    p, m = W.cfg2_probe(), W.cfg2_medium()
+    s, r = W.cfg2_scatterers(20_000, seed=3)
+    plan = F.simus_precompute(s, r, np.zeros(128), p, m)
+    full = np64(F.simus_compute(s, r, np.zeros(128), plan, p, m).spectrum)
+    a = np64(F.simus_compute(s[:7000], r[:7000], np.zeros(128), plan, p, m).spectrum)
+    b = np64(F.simus_compute(s[7000:], r[7000:], np.zeros(128), plan, p, m).spectrum)
+    assert G.rel_l2(a + b, full) < 1e-5
+
+
+def test_deterministic_bitwise():
+    import fastsimus_gb300 as F
+    from fastsimus_gb300 import workloads as W
+
+    p, m = W.cfg1_probe(), W.cfg1_medium()
+    s, r = W.cfg1_scatterers(3000, seed=9)
+    plan = F.simus_precompute(s, r, np.zeros(64), p, m)
+    x = F.simus_compute(s, r, np.zeros(64), plan, p, m).spectrum
+    y = F.simus_compute(s, r, np.zeros(64), plan, p, m).spectrum
+    assert torch.equal(x, y)
+
+
+def test_ffd_unsupported_raises():
+    import fastsimus_gb300 as F
+
+    g = G.load("simus_small_ffd")
+    with pytest.raises(NotImplementedError):
+        F.simus(g.scatterers, g.rc, g.delays, g.params, g.medium, full_frequency_directivity=True)
+
+
+def test_cpu_strategies_raise():
+    import fastsimus_gb300 as F
+
+    g = G.load("simus_small_rigid")
+    with pytest.raises(NotImplementedError):
+        F.simus(g.scatterers, g.rc, g.delays, g.params, g.medium, strategy="python")
+
+
+def test_bad_arguments_raise_before_launch():
+    import fastsimus_gb300 as F
+
+    g = G.load("simus_small_rigid")
+    with pytest.raises(ValueError):
+        F.simus(g.scatterers, g.rc[:-1], g.delays, g.params, g.medium)
+    with pytest.raises(ValueError):
+        F.simus(g.scatterers, g.rc, g.delays[:-1], g.params, g.medium)
