@@ -74,6 +74,12 @@ def _cpu_info():
 # CPU baseline: the oracle (FP64 NumPy port of the reference's PYTHON strategy)
 # ------------------------------------------------------------------------------------------
 
+def _single_thread_blas():
+    """Oracle workers run one process per core; each must use one BLAS/OpenMP thread."""
+    for v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[v] = "1"
+
+
 def _oracle_simus_shard(args):
     import oracle.fastsimus_fp64 as O
 
@@ -109,13 +115,13 @@ def cpu_frame_time(pool, n_workers, scat, rc, grid_pts, delays, plan, pplan, par
     return (t1 - t0) * scat.shape[0] / s_sample + (t2 - t1) * grid_pts.shape[0] / g_sample
 
 
-def make_workload():
+def make_workload(n_scat=200_000, grid_nx=256, grid_nz=512):
     from fastsimus_gb300 import workloads as W
     from fastsimus_gb300.plan import pfield_precompute, simus_precompute
 
     params, medium = W.cfg2_probe(), W.cfg2_medium()
-    scat, rc = W.cfg2_scatterers()
-    grid = W.cfg2_grid()
+    scat, rc = W.cfg2_scatterers(n_scat)
+    grid = W.cfg2_grid(grid_nx, grid_nz)
     delays = np.zeros(params.n_elements)
     t0 = time.perf_counter()
     plan = simus_precompute(scat, rc, delays, params, medium)
@@ -142,9 +148,10 @@ def run_reference_arm(args, rank, world):
         return
     import multiprocessing as mp
 
-    params, medium, scat, rc, grid, delays, plan, pplan, _ = make_workload()
+    params, medium, scat, rc, grid, delays, plan, pplan, _ = make_workload(args.scatterers, args.grid_nx, args.grid_nz)
     gpts = grid.reshape(-1, 2)
     model, cores = _cpu_info()
+    _single_thread_blas()
     ctx = mp.get_context("spawn")
     s_sample, g_sample = args.cpu_scatterers, args.cpu_points
     with ctx.Pool(cores) as pool:
@@ -279,7 +286,8 @@ def run_gpu_arm(args, rank, world):
 
         dist.init_process_group("nccl", device_id=device)
 
-    params, medium, scat, rc, grid, delays, plan, pplan, t_plan = make_workload()
+    params, medium, scat, rc, grid, delays, plan, pplan, t_plan = make_workload(args.scatterers, args.grid_nx,
+                                                                                 args.grid_nz)
     n_scat, n_grid = scat.shape[0], grid.shape[0] * grid.shape[1]
 
     # device-resident inputs
@@ -323,6 +331,14 @@ def run_gpu_arm(args, rank, world):
     value = frames / (dev_ms * 1e-3)
     simus_ms = timer.elapsed_ms("fsg_simus")
     pfield_ms = timer.elapsed_ms("fsg_pfield")
+
+    if args.no_e2e:
+        if rank == 0:
+            print(json.dumps({"value": value, "simus_ms": float(np.mean(simus_ms)),
+                              "pfield_ms": float(np.mean(pfield_ms)), "note": "profiling run (no e2e)"}), flush=True)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
 
     # end-to-end through the public API with host (pinned) buffers
     scat_h = torch.as_tensor(scat).pin_memory()
@@ -390,6 +406,7 @@ def run_gpu_arm(args, rank, world):
         import multiprocessing as mp
 
         model, cores = _cpu_info()
+        _single_thread_blas()
         ctx = mp.get_context("spawn")
         with ctx.Pool(cores) as pool:
             cpu_frame_time(pool, cores, scat, rc, grid.reshape(-1, 2), delays, plan, pplan, params, medium,
@@ -411,9 +428,13 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--cpu-scatterers", type=int, default=2048)
-    ap.add_argument("--cpu-points", type=int, default=4096)
+    ap.add_argument("--cpu-scatterers", type=int, default=8192)
+    ap.add_argument("--cpu-points", type=int, default=16384)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="device timing only (profiling runs)")
+    ap.add_argument("--scatterers", type=int, default=200_000, help="smaller values make profiling cases")
+    ap.add_argument("--grid-nx", type=int, default=256)
+    ap.add_argument("--grid-nz", type=int, default=512)
     args = ap.parse_args()
     rank, world = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1)
     if args.impl == "reference":

@@ -104,7 +104,7 @@ size_t tables_bytes(int E, int U, int F) {
   const int n_anchor = (F + kAnchor - 1) / kAnchor;
   size_t b = 0;
   b += align256((size_t)n_src * 16);
-  b += align256((size_t)E * 4);
+  b += align256((size_t)E * 8);
   b += align256((size_t)F * 8);
   b += align256((size_t)F * 4);
   b += align256((size_t)F * 8);
@@ -120,7 +120,7 @@ Tables carve_tables(unsigned char* base, int E, int U, int F) {
   Tables t;
   size_t o = 0;
   t.src_pos = reinterpret_cast<float4*>(base + o); o += align256((size_t)n_src * 16);
-  t.theta_e = reinterpret_cast<float*>(base + o); o += align256((size_t)E * 4);
+  t.rot_e = reinterpret_cast<float2*>(base + o); o += align256((size_t)E * 8);
   t.kf = reinterpret_cast<float2*>(base + o); o += align256((size_t)F * 8);
   t.af = reinterpret_cast<float*>(base + o); o += align256((size_t)F * 4);
   t.pp = reinterpret_cast<float2*>(base + o); o += align256((size_t)F * 8);

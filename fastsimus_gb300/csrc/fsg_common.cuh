@@ -17,7 +17,8 @@
 
 namespace fsg {
 
-constexpr int kAnchor = 32;     // frequency steps between exact anchors
+constexpr int kAnchor = 32;     // frequency steps between exact anchors (receive side, tables)
+constexpr int kTxAnchor = 64;   // frequency steps between exact anchors on the transmit side
 constexpr int kSrcPerThread = 16;
 constexpr int kThreads = 256;
 
@@ -124,43 +125,54 @@ struct SweepConst {
   int ffd;          // full-frequency directivity (directivity applied per frequency)
 };
 
+// sin(x)/x: Taylor series for |x| < 2 (truncation error < 3e-9), sinf(x)/x beyond.
+__device__ __forceinline__ float sinc_rad(float x) {
+  if (fabsf(x) < 2.0f) {
+    const float x2 = x * x;
+    float p = -1.0f / 6227020800.0f;  // -1/13!
+    p = fmaf(p, x2, 1.0f / 39916800.0f);
+    p = fmaf(p, x2, -1.0f / 362880.0f);
+    p = fmaf(p, x2, 1.0f / 5040.0f);
+    p = fmaf(p, x2, -1.0f / 120.0f);
+    p = fmaf(p, x2, 1.0f / 6.0f);
+    return fmaf(-p, x2, 1.0f);  // 1 - x^2/6 + x^4/120 - ...
+  }
+  return __fdiv_rn(sinf(x), x);
+}
+
 // Geometry of one (point, source) pair: clipped distance (double-float), amplitude
-// obliquity * directivity / sqrt(r) / n_sub, per-step multiplier exp((-d_alpha + i d_k) r),
-// and sin(theta) (needed for full-frequency directivity).
-// Follows _distances_and_angles (_pfield_math.py:70-118), _obliquity_factor (:165-199),
-// the centre-frequency sinc (simus.py:310-313) and the step of _init_exponentials (:240-245).
+// obliquity * directivity / sqrt(r) / n_sub and the per-step multiplier
+// exp((-d_alpha + i d_k) r).  Follows _distances_and_angles (_pfield_math.py:70-118),
+// _obliquity_factor (:165-199), the centre-frequency sinc (simus.py:310-313) and the step of
+// _init_exponentials (:240-245).  The angle theta = asin(dx / r) - theta_e enters only
+// through sin(theta) and cos(theta), formed from a = dx / r and the element rotation
+// (cos theta_e, sin theta_e); |theta| >= pi/2 (the 1e-16 horizon floor) is cos(theta) <= 0.
 struct SrcGeo {
   float r_hi, r_lo, amp;
   float2 step;
-  float sin_theta;
 };
 
-__device__ __forceinline__ SrcGeo source_geometry(dfl xs, dfl zs, float4 sp, float theta_e, const SweepConst& C) {
+__device__ __forceinline__ SrcGeo source_geometry(dfl xs, dfl zs, float4 sp, float2 rot, const SweepConst& C) {
   dfl dx = df_add(xs, dfl{-sp.x, -sp.y});
   dfl dz = df_add(zs, dfl{-sp.z, -sp.w});
   dfl r = df_sqrt(df_add(df_sqr(dx), df_sqr(dz)));
-  // angle from the unclipped distance, with the reference's 1e-16 guards
-  float a = __fdiv_rn(dx.hi + 1e-16f, r.hi + 1e-16f);
+  // a = (dx + 1e-16) / (r + 1e-16) on the unclipped distance; a = 1 when the point sits on the source
+  float a = (r.hi > 0.0f) ? __fdiv_rn(dx.hi, r.hi) : 1.0f;
   a = fminf(1.0f, fmaxf(-1.0f, a));
-  float th = asinf(a) - theta_e;
+  const float ca = sqrtf((1.0f - a) * (1.0f + a));  // cos(asin(a)) >= 0
+  const float sth = fmaf(a, rot.x, -ca * rot.y);   // sin(asin(a) - theta_e)
+  const float cth = fmaf(ca, rot.x, a * rot.y);    // cos(asin(a) - theta_e)
   if (r.hi < C.min_dist.x || (r.hi == C.min_dist.x && r.lo < C.min_dist.y)) r = dfl{C.min_dist.x, C.min_dist.y};
-  float sth, cth;
-  sincosf(th, &sth, &cth);
   float ob = (C.baffle == 0) ? cth : ((C.baffle == 1) ? 1.0f : __fdiv_rn(cth, cth + C.baffle_val));
-  if (fabsf(th) >= kHalfPiF) ob = 1e-16f;
-  float dir = 1.0f;
-  if (!C.ffd) {
-    float x = C.dir_coef * sth;
-    dir = (x == 0.0f) ? 1.0f : __fdiv_rn(sinf(x), x);
-  }
+  if (cth <= 0.0f) ob = 1e-16f;
+  const float dir = C.ffd ? 1.0f : sinc_rad(C.dir_coef * sth);
   SrcGeo g;
   g.r_hi = r.hi;
   g.r_lo = r.lo;
   g.amp = ob * dir * rsqrtf(r.hi) * C.inv_nsub;
-  float mag = expf(-C.dalpha * r.hi);
-  float2 cis = df_cis_accurate(C.dk, r.hi, r.lo);
+  const float mag = (C.dalpha != 0.0f) ? expf(-C.dalpha * r.hi) : 1.0f;
+  const float2 cis = df_cis_accurate(C.dk, r.hi, r.lo);
   g.step = make_float2(mag * cis.x, mag * cis.y);
-  g.sin_theta = sth;
   return g;
 }
 

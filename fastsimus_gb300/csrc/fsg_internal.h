@@ -11,7 +11,7 @@ namespace fsg {
 
 struct Tables {
   float4* src_pos;   // [n_src] x_hi, x_lo, z_hi, z_lo
-  float* theta_e;    // [E]
+  float2* rot_e;     // [E] (cos theta_e, sin theta_e)
   float2* kf;        // [F] k_f double-float
   float* af;         // [F] attenuation Np/m at f
   float2* pp;        // [F] pulse * probe

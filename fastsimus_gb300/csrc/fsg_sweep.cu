@@ -58,7 +58,7 @@ __global__ void setup_tables(SetupArgs a) {
     double sz = ze + off * sin(-te);
     dfl hx = split_double(sx), hz = split_double(sz);
     a.t.src_pos[i] = make_float4(hx.hi, hx.lo, hz.hi, hz.lo);
-    if (u == 0) a.t.theta_e[e] = (float)te;
+    if (u == 0) a.t.rot_e[e] = make_float2((float)cos(te), (float)sin(te));
   }
   if (i < a.F) {
     double f = a.f0 + i * a.df;
@@ -126,45 +126,45 @@ __device__ __forceinline__ void tx_tile(const BandArgs& A, const SmemLayout& L, 
   const float* aa = reinterpret_cast<const float*>(sm + L.off_aa);
   const float2* da = reinterpret_cast<const float2*>(sm + L.off_da);
 
-  const dfl xs = load_coord(A.pts + 2 * p_idx);
-  const dfl zs = load_coord(A.pts + 2 * p_idx + 1);
-
-  float2 G[kSrcPerThread];
-  float2 S[kSrcPerThread];
-#pragma unroll
-  for (int i = 0; i < kSrcPerThread; ++i) {
-    const int src = g * kSrcPerThread + i;
-    G[i] = make_float2(0.f, 0.f);
-    S[i] = make_float2(0.f, 0.f);
-    if (src < A.n_src) {
-      const int e = src / A.U, u = src - e * A.U;
-      const int row = u * A.E + e;
-      SrcGeo geo = source_geometry(xs, zs, A.t.src_pos[src], A.t.theta_e[e], A.C);
-      b_rhi[row * L.pitch + sl] = geo.r_hi;
-      b_rlo[row * L.pitch + sl] = geo.r_lo;
-      b_amp[row * L.pitch + sl] = geo.amp;
-      b_st[row * L.pitch + sl] = geo.step;
-      S[i] = cmul(geo.step, A.t.dstep[e]);
-      G[i] = cmul(anchor_value(geo.r_hi, geo.r_lo, geo.amp, ka[0], aa[0]), da[e]);
-    }
-  }
-  const int na = A.fb / kAnchor;
-  for (int m = 0; m < na; ++m) {
-    if (m > 0) {
-#pragma unroll
-      for (int i = 0; i < kSrcPerThread; ++i) {
-        const int src = g * kSrcPerThread + i;
-        if (src < A.n_src) {
-          const int e = src / A.U, u = src - e * A.U;
-          const int row = u * A.E + e;
-          G[i] = cmul(anchor_value(b_rhi[row * L.pitch + sl], b_rlo[row * L.pitch + sl], b_amp[row * L.pitch + sl],
-                                   ka[m], aa[m]),
-                      da[m * A.E + e]);
-        }
+  // 1. geometry of my sources, parked in shared memory (rolled loop: one copy of the code)
+  {
+    const dfl xs = load_coord(A.pts + 2 * p_idx);
+    const dfl zs = load_coord(A.pts + 2 * p_idx + 1);
+#pragma unroll 1
+    for (int i = 0; i < kSrcPerThread; ++i) {
+      const int src = g * kSrcPerThread + i;
+      if (src < A.n_src) {
+        const int e = src / A.U, u = src - e * A.U;
+        const int idx = (u * A.E + e) * L.pitch + sl;
+        const SrcGeo geo = source_geometry(xs, zs, A.t.src_pos[src], A.t.rot_e[e], A.C);
+        b_rhi[idx] = geo.r_hi;
+        b_rlo[idx] = geo.r_lo;
+        b_amp[idx] = geo.amp;
+        b_st[idx] = geo.step;
       }
     }
+  }
+  // 2. transmit sweep: exact anchor every kTxAnchor steps, FP32 recurrence in between
+  float2 G[kSrcPerThread];
+  float2 S[kSrcPerThread];
+  const int n_tx_anchor = (A.fb + kTxAnchor - 1) / kTxAnchor;
+  for (int m = 0; m < n_tx_anchor; ++m) {
+    const int am = m * (kTxAnchor / kAnchor);  // index into the band's kAnchor-spaced tables
+#pragma unroll
+    for (int i = 0; i < kSrcPerThread; ++i) {
+      const int src = g * kSrcPerThread + i;
+      G[i] = make_float2(0.f, 0.f);
+      if (m == 0) S[i] = make_float2(0.f, 0.f);
+      if (src < A.n_src) {
+        const int e = src / A.U, u = src - e * A.U;
+        const int idx = (u * A.E + e) * L.pitch + sl;
+        G[i] = cmul(anchor_value(b_rhi[idx], b_rlo[idx], b_amp[idx], ka[am], aa[am]), da[am * A.E + e]);
+        if (m == 0) S[i] = cmul(b_st[idx], A.t.dstep[e]);
+      }
+    }
+    const int n_steps = min(kTxAnchor, A.fb - m * kTxAnchor);
 #pragma unroll 2
-    for (int j = 0; j < kAnchor; ++j) {
+    for (int j = 0; j < n_steps; ++j) {
       float2 ps = G[0];
       G[0] = cmul(G[0], S[0]);
 #pragma unroll
@@ -176,7 +176,7 @@ __device__ __forceinline__ void tx_tile(const BandArgs& A, const SmemLayout& L, 
         ps.x += __shfl_xor_sync(0xffffffffu, ps.x, off);
         ps.y += __shfl_xor_sync(0xffffffffu, ps.y, off);
       }
-      if (g == 0) sink(m * kAnchor + j, ps);
+      if (g == 0) sink(m * kTxAnchor + j, ps);
     }
   }
 }
