@@ -58,6 +58,10 @@ _SIGNATURES = {
                                                     ctypes.c_int64]),
     "fsg_pfield": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgMedium), ctypes.POINTER(FsgFreqPlan),
                                     _P, ctypes.c_int64, _P, _P, ctypes.c_int32, _P, _P, ctypes.c_size_t, _P]),
+    "fsg_simus_noalloc": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgMedium),
+                                           ctypes.POINTER(FsgFreqPlan), _P, _P, ctypes.c_int64, _P, _P, ctypes.c_int32,
+                                           ctypes.c_int32, _P, _P]),
+    "fsg_simus_noalloc_scratch_bytes": (ctypes.c_size_t, []),
     "fsg_fp32_fma_probe": (ctypes.c_int32, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
                                             _P]),
 }

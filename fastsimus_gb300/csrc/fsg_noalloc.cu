@@ -1,0 +1,81 @@
+// fsg_simus_noalloc: the plain simus sweep for callers that cannot allocate device memory.
+//
+// Some callers of this library cannot call cudaMalloc: a plugin inside a host application
+// that owns all device memory and hands the plugin only its input and output buffers (a
+// scanner's real-time processing chain, an inference-server backend with a fixed memory
+// budget), or code that must not synchronise the device mid-stream, which cudaMalloc/cudaFree
+// may do.  This entry point takes the same inputs and outputs as fsg_simus but no workspace:
+// its scratch (the per-frequency tables and the per-slice partial spectra) lives in the
+// file-scope device array below.
+//
+// Limits and behaviour:
+//   - The scratch is kNoAllocScratchBytes (16 MiB).  Requests whose fsg_simus workspace would be
+//     larger are rejected with FSG_EINVAL and a message; nothing is launched.  On a 152-SM
+//     GB300 every probe this library supports (n_elements <= 256) fits for any scatterer count
+//     as long as the plan has at most a few thousand frequencies.
+//   - The array is part of this library's device image, so every GPU that loads the library
+//     holds the 16 MiB until the process exits.
+//   - Host code cannot use the array's name as a device address.  The first call on each
+//     device, with that device current, asks the runtime for the address
+//     (cudaGetSymbolAddress) and caches it; make that first call before any stream capture.
+//   - All calls share the array and it keeps the last call's contents.  Every byte the sweep
+//     reads is written earlier in the same call (tables by the set-up kernel, partials by the
+//     band kernel, one entry per (slice, frequency, element)), so nothing has to start at zero.
+//   - Calls whose work overlaps on the GPU (different streams, or different host threads on
+//     one device) race on the shared scratch and corrupt each other's results; serialise them.
+//   - The call allocates nothing: no cudaMalloc, no cudaFree, no allocating library routine.
+
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "../../include/fsgb300.h"
+#include "fsg_internal.h"
+
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kMaxDevices] = {};
+
+int scratch_address(void** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fsg::check_cuda(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) return fsg::set_error(FSG_EINVAL, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return fsg::check_cuda(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return FSG_OK;
+}
+
+}  // namespace
+
+extern "C" size_t fsg_simus_noalloc_scratch_bytes(void) { return kNoAllocScratchBytes; }
+
+extern "C" int32_t fsg_simus_noalloc(const FsgProbe* probe, const FsgMedium* medium, const FsgFreqPlan* plan,
+                                     const double* scat_xz, const double* rc, int64_t n_scat, const double* delays,
+                                     const double* apod, int32_t full_frequency_directivity, int32_t out_layout,
+                                     void* out, void* stream) {
+  if (!probe || !plan) return fsg::set_error(FSG_EINVAL, "probe and plan must be non-NULL");
+  const size_t need = fsg_simus_workspace_size(probe, plan, n_scat);
+  if (need == 0) return fsg::set_error(FSG_EINVAL, "fsg_simus_noalloc: cannot size the scratch for this request");
+  if (need > kNoAllocScratchBytes)
+    return fsg::set_error(FSG_EINVAL,
+                          "fsg_simus_noalloc: this request needs %zu bytes of scratch but the static scratch holds "
+                          "%zu bytes; use fsg_simus with a caller-provided workspace",
+                          need, kNoAllocScratchBytes);
+  void* scratch = nullptr;
+  int st = scratch_address(&scratch);
+  if (st != FSG_OK) return st;
+  return fsg_simus(probe, medium, plan, scat_xz, rc, n_scat, delays, apod, full_frequency_directivity, out_layout,
+                   out, scratch, kNoAllocScratchBytes, stream);
+}

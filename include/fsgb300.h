@@ -131,6 +131,23 @@ int32_t fsg_pfield(const FsgProbe* probe, const FsgMedium* medium, const FsgFreq
                    int32_t full_frequency_directivity, float* out,
                    void* workspace, size_t workspace_bytes, void* stream);
 
+/*
+ * fsg_simus without a workspace argument, for callers that cannot allocate device memory
+ * (for example a plugin whose host application owns all device memory and passes only input
+ * and output buffers).  No counterpart in the reference: it is fsg_simus running on a 16 MiB
+ * scratch array held in the library's own device image (see fsg_simus_noalloc_scratch_bytes).
+ * Requests needing more scratch fail with FSG_EINVAL.  The first call on a device looks up
+ * the array's device address; make it before any stream capture.  All calls share the
+ * scratch: calls that overlap on the GPU race, so serialise them.
+ */
+int32_t fsg_simus_noalloc(const FsgProbe* probe, const FsgMedium* medium, const FsgFreqPlan* plan,
+                          const double* scat_xz, const double* rc, int64_t n_scat,
+                          const double* delays, const double* apod,
+                          int32_t full_frequency_directivity, int32_t out_layout, void* out, void* stream);
+
+/* Size in bytes of fsg_simus_noalloc's static scratch (no counterpart in the reference). */
+size_t fsg_simus_noalloc_scratch_bytes(void);
+
 /* Measurement utility, no counterpart in the reference: launches `blocks` x 256 threads of
  * independent FP32 FMA chains (`iters` iterations) and reports the FLOPs it performs, so a
  * caller can time it with events and state the device's FP32 FMA roofline.  `out` must hold
