@@ -45,6 +45,16 @@ class FsgFreqPlan(ctypes.Structure):
                 ("pulse_spectrum", ctypes.c_void_p), ("probe_spectrum", ctypes.c_void_p)]
 
 
+class FsgPhantom(ctypes.Structure):
+    _fields_ = [("scat_xz", ctypes.c_void_p), ("rc", ctypes.c_void_p), ("n_scat", ctypes.c_int64),
+                ("plan", FsgFreqPlan), ("out", ctypes.c_void_p)]
+
+
+class FsgBatchTuning(ctypes.Structure):
+    _fields_ = [("freqs_per_item", ctypes.c_int32), ("chunk_scatterers", ctypes.c_int32),
+                ("ctas_per_sm", ctypes.c_int32), ("reserved0", ctypes.c_int32)]
+
+
 _P = ctypes.c_void_p
 _SIGNATURES = {
     "fsg_abi_version": (ctypes.c_int32, []),
@@ -58,6 +68,12 @@ _SIGNATURES = {
                                                     ctypes.c_int64]),
     "fsg_pfield": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgMedium), ctypes.POINTER(FsgFreqPlan),
                                     _P, ctypes.c_int64, _P, _P, ctypes.c_int32, _P, _P, ctypes.c_size_t, _P]),
+    "fsg_simus_batched_workspace_size": (ctypes.c_size_t, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgPhantom),
+                                                           ctypes.c_int32, ctypes.c_int32,
+                                                           ctypes.POINTER(FsgBatchTuning)]),
+    "fsg_simus_batched": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgMedium),
+                                           ctypes.POINTER(FsgPhantom), ctypes.c_int32, _P, _P, ctypes.c_int32,
+                                           ctypes.POINTER(FsgBatchTuning), _P, ctypes.c_size_t, _P]),
     "fsg_simus_noalloc": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgMedium),
                                            ctypes.POINTER(FsgFreqPlan), _P, _P, ctypes.c_int64, _P, _P, ctypes.c_int32,
                                            ctypes.c_int32, _P, _P]),

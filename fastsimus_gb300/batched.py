@@ -1,0 +1,250 @@
+"""Many transmits x many phantoms in one persistent launch (libfsgb300 ``fsg_simus_batched``).
+
+The reference simulates a multi-transmit acquisition with a caller loop: one plan per phantom,
+computed with ``simus_precompute`` on the firing whose delay span is largest, then one
+``simus_compute`` per firing with that plan (``tests/_picmus_phantom_shared.py:319-367``), and
+RF stacked as (samples, channels, firings).  ``simus_batched`` keeps exactly that plan rule
+and output layout, but computes every (phantom, firing) in a single launch: each Green's term
+is generated once and contracted with all firings.
+
+``BatchedSimus`` keeps inputs, plans, workspace and outputs resident for repeated runs,
+captures the whole batch (set-up, persistent sweep, reduction, cuFFT irfft, gate) in a CUDA
+graph, and picks tile shapes with ``autotune``.
+"""
+
+from __future__ import annotations
+
+import json
+import os
+import time
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+import torch
+
+from fastsimus_gb300 import _device, _native
+from fastsimus_gb300.params import MediumParams, TransducerParams
+from fastsimus_gb300.plan import SimusPlan, simus_precompute
+from fastsimus_gb300.simus import SimusResult
+
+_DEFAULT_MEDIUM = MediumParams()
+
+
+@dataclass(frozen=True)
+class BatchTuning:
+    """Tile shapes of the batched sweep: frequencies per work item (1 or 2), scatterers per
+    work item, persistent CTAs per SM."""
+
+    freqs_per_item: int = 2
+    chunk_scatterers: int = 32768
+    ctas_per_sm: int = 1
+
+    def to_c(self) -> _native.FsgBatchTuning:
+        return _native.FsgBatchTuning(self.freqs_per_item, self.chunk_scatterers, self.ctas_per_sm, 0)
+
+
+def shared_plan(scatterers, rc, delays_list, params: TransducerParams, medium: MediumParams, **plan_kw) -> SimusPlan:
+    """The reference's multi-firing plan rule: precompute on the firing with the largest delay
+    span (tests/_picmus_phantom_shared.py:329-347)."""
+    spans = [float(np.ptp(np.nan_to_num(np.asarray(d, dtype=np.float64)))) for d in delays_list]
+    return simus_precompute(scatterers, rc, delays_list[int(np.argmax(spans))], params, medium, **plan_kw)
+
+
+def _gate(rf: torch.Tensor) -> torch.Tensor:
+    """Smooth -100 dB gate of simus.py:359-365, with each firing's own peak (rf: T x N x E)."""
+    th = 1e-5
+    mag = rf.abs()
+    rel = mag / (mag.amax(dim=(1, 2), keepdim=True) + 1e-30)
+    return rf * (0.5 * (1.0 + torch.tanh((rel - th) / (th / 10.0))))
+
+
+class BatchedSimus:
+    """A resident batch: phantoms (scatterers, rc), one delay law per firing, shared plans."""
+
+    def __init__(self, phantoms, delays, params: TransducerParams, medium: MediumParams = _DEFAULT_MEDIUM, *,
+                 plans: list[SimusPlan] | None = None, tx_apodization=None, tuning: BatchTuning | None = None,
+                 fs: float | None = None, device: torch.device | None = None):
+        self.device = device or _device.require_cuda()
+        self.lib = _native.load()
+        self.params, self.medium = params, medium
+        d = np.asarray(delays, dtype=np.float64)
+        if d.ndim != 2 or d.shape[1] != params.n_elements:
+            raise ValueError(f"delays must be (n_tx, {params.n_elements}), got {d.shape}")
+        self.n_tx = d.shape[0]
+        self.phantoms = []
+        for scat, rc in phantoms:
+            s = _device.to_dev_f64(scat, self.device).reshape(-1, 2).contiguous()
+            r = _device.to_dev_f64(rc, self.device).reshape(-1).contiguous()
+            if r.shape[0] != s.shape[0]:
+                raise ValueError("rc and scatterers differ in length")
+            self.phantoms.append((s, r))
+        if plans is None:
+            plans = [shared_plan(s.cpu().numpy(), r.cpu().numpy(), list(d), params, medium, fs=fs)
+                     for s, r in self.phantoms]
+        self.plans = plans
+        self.delays = torch.as_tensor(d, device=self.device).contiguous()
+        self.apod = None
+        if tx_apodization is not None:
+            a = np.broadcast_to(np.asarray(tx_apodization, dtype=np.float64), d.shape)
+            self.apod = torch.as_tensor(np.ascontiguousarray(a), device=self.device)
+        self.tabs = [_device.plan_tables(p, self.device) for p in plans]
+        self.outs = [torch.empty((self.n_tx, p.n_freq_full, params.n_elements), dtype=torch.complex64,
+                                 device=self.device) for p in plans]
+        self.probe = _native.make_probe(params, plans[0].n_sub)
+        if any(p.n_sub != plans[0].n_sub for p in plans):
+            raise ValueError("all phantoms of a batch must share n_sub")
+        self.med = _native.make_medium(medium)
+        self.graph = None
+        self.set_tuning(tuning or BatchTuning())
+
+    # -- native call -------------------------------------------------------------------------
+    def _fsg_phantoms(self):
+        arr = (_native.FsgPhantom * len(self.phantoms))()
+        for i, ((s, r), p, t, o) in enumerate(zip(self.phantoms, self.plans, self.tabs, self.outs)):
+            arr[i].scat_xz = s.data_ptr()
+            arr[i].rc = r.data_ptr()
+            arr[i].n_scat = int(s.shape[0])
+            arr[i].plan = t.fsg_plan(p)
+            arr[i].out = o.data_ptr()
+        return arr
+
+    def set_tuning(self, tuning: BatchTuning):
+        self.tuning = tuning
+        self._ph = self._fsg_phantoms()
+        nbytes = self.lib.fsg_simus_batched_workspace_size(self.probe, self._ph, len(self.phantoms), self.n_tx,
+                                                           tuning.to_c())
+        if nbytes == 0:
+            raise ValueError("fsg_simus_batched_workspace_size rejected the batch")
+        self.ws = _device.workspace(nbytes, self.device)
+        self.graph = None
+
+    def launch_sweep(self):
+        """Enqueue the batched sweep on the current stream (outputs: corrected spectra)."""
+        with torch.cuda.device(self.device), _device.timed("fsg_simus_batched", self.device):
+            st = self.lib.fsg_simus_batched(self.probe, self.med, self._ph, len(self.phantoms),
+                                            self.delays.data_ptr(), self.apod.data_ptr() if self.apod is not None
+                                            else None, self.n_tx, self.tuning.to_c(), self.ws.data_ptr(),
+                                            self.ws.numel(), _device.stream_handle(self.device))
+        _native.check(st)
+
+    def _finish(self):
+        self.rfs = []
+        for plan, out in zip(self.plans, self.outs):
+            rf = torch.fft.irfft(torch.conj(out), n=plan.n_fft, dim=1)[:, : (plan.n_fft + 1) // 2]
+            self.rfs.append(_gate(rf))
+
+    def run(self) -> list[SimusResult]:
+        """One pass (eager launches).  Returns, per phantom, rf (n_samples, E, n_tx) and
+        spectrum (n_freq_full, E, n_tx) -- the reference helper's (samples, channels, firings)."""
+        self.launch_sweep()
+        self._finish()
+        return self.results()
+
+    def results(self) -> list[SimusResult]:
+        return [SimusResult(rf=rf.permute(1, 2, 0), spectrum=o.permute(1, 2, 0)) for rf, o in zip(self.rfs, self.outs)]
+
+    # -- CUDA graph ----------------------------------------------------------------------------
+    def capture(self):
+        """Record the whole batch in a CUDA graph (after one eager warm-up pass)."""
+        self.run()
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream(self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(s):
+            self.run()  # warm the capture stream (cuFFT plans, attributes)
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        torch.cuda.synchronize(self.device)
+        with torch.cuda.graph(g):
+            self.launch_sweep()
+            self._finish()
+        self.graph = g
+        return g
+
+    def replay(self) -> list[SimusResult]:
+        if self.graph is None:
+            self.capture()
+        self.graph.replay()
+        return self.results()
+
+    # -- autotuner -----------------------------------------------------------------------------
+    def autotune(self, candidates: list[BatchTuning] | None = None, reps: int = 1, cache: bool = True) -> BatchTuning:
+        """Time each candidate tiling on this batch with CUDA events and keep the fastest.
+        Results are cached by (E, n_sub, n_tx, n_phantoms, log2 total scatterers, F bucket) in
+        memory and in ``$FASTSIMUS_GB300_CACHE`` (default ``~/.cache/fastsimus_gb300``)."""
+        key = self._tune_key()
+        table = _load_cache() if cache else {}
+        if cache and key in table:
+            best = BatchTuning(**table[key])
+            self.set_tuning(best)
+            return best
+        if candidates is None:
+            total = sum(int(s.shape[0]) for s, _ in self.phantoms)
+            chunks = sorted({c for c in (8192, 16384, 32768, 65536, 131072) if c < 2 * max(total, 64)} or {8192})
+            candidates = [BatchTuning(fb, c, 1) for fb in (1, 2) for c in chunks[:: max(1, len(chunks) // 2)]]
+        timings = []
+        for cand in candidates:
+            self.set_tuning(cand)
+            self.launch_sweep()  # warm-up
+            torch.cuda.synchronize(self.device)
+            st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            st.record()
+            for _ in range(reps):
+                self.launch_sweep()
+            en.record()
+            torch.cuda.synchronize(self.device)
+            timings.append((st.elapsed_time(en) / reps, cand))
+        best = min(timings, key=lambda x: x[0])[1]
+        self.tune_log = [(t, c.__dict__) for t, c in timings]
+        self.set_tuning(best)
+        if cache:
+            table[key] = best.__dict__
+            _save_cache(table)
+        return best
+
+    def _tune_key(self) -> str:
+        total = sum(int(s.shape[0]) for s, _ in self.phantoms)
+        fbar = int(np.mean([p.selected_freqs.shape[0] for p in self.plans]))
+        return (f"E{self.params.n_elements}-U{self.plans[0].n_sub}-T{self.n_tx}-P{len(self.phantoms)}"
+                f"-S{int(np.log2(max(total, 1)))}-F{fbar // 64}")
+
+
+def _cache_path() -> Path:
+    root = Path(os.environ.get("FASTSIMUS_GB300_CACHE", Path.home() / ".cache" / "fastsimus_gb300"))
+    return root / "autotune.json"
+
+
+_mem_cache: dict = {}
+
+
+def _load_cache() -> dict:
+    if _mem_cache:
+        return _mem_cache
+    try:
+        _mem_cache.update(json.loads(_cache_path().read_text()))
+    except Exception:
+        pass
+    return _mem_cache
+
+
+def _save_cache(table: dict):
+    _mem_cache.update(table)
+    try:
+        p = _cache_path()
+        p.parent.mkdir(parents=True, exist_ok=True)
+        tmp = p.with_suffix(f".{os.getpid()}.{time.time_ns()}.tmp")
+        tmp.write_text(json.dumps(_mem_cache, indent=1, sort_keys=True))
+        os.replace(tmp, p)
+    except OSError:
+        pass
+
+
+def simus_batched(phantoms, delays, params: TransducerParams, medium: MediumParams = _DEFAULT_MEDIUM, *,
+                  plans: list[SimusPlan] | None = None, tx_apodization=None, fs: float | None = None,
+                  tuning: BatchTuning | None = None) -> list[SimusResult]:
+    """RF of every (phantom, firing): ``phantoms`` is a list of (scatterers (S, 2), rc (S,)),
+    ``delays`` is (n_tx, n_elements).  Returns per phantom rf (n_samples, E, n_tx) float32 and
+    spectrum (n_freq_full, E, n_tx) complex64, on the GPU."""
+    return BatchedSimus(phantoms, delays, params, medium, plans=plans, tx_apodization=tx_apodization,
+                        tuning=tuning, fs=fs).run()

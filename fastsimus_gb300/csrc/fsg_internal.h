@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include "fsg_common.cuh"
+#include "../../include/fsgb300.h"
 
 namespace fsg {
 
@@ -87,6 +88,8 @@ __global__ void pfield_reduce(const float* __restrict__ partial, int n_bands, in
                               float* __restrict__ out);
 
 int set_error(int code, const char* fmt, ...);
+SweepConst make_sweep_const(const FsgProbe* p, const FsgMedium* m, const FsgFreqPlan* plan, int ffd);
+void convex_geometry(const FsgProbe* p, int* convex, double* apex, double* radius2);
 int check_cuda(cudaError_t err, const char* what);
 
 }  // namespace fsg

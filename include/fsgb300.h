@@ -131,6 +131,43 @@ int32_t fsg_pfield(const FsgProbe* probe, const FsgMedium* medium, const FsgFreq
                    int32_t full_frequency_directivity, float* out,
                    void* workspace, size_t workspace_bytes, void* stream);
 
+/* One phantom of a batched multi-transmit sweep: its scatterers, the plan shared by all of its
+ * transmits, and its output, complex64 [n_tx][plan.n_freq_full][n_elements] (selected band times
+ * correction_factor, zero-padded: one FSG_OUT_FULL_CORRECTED spectrum per transmit). */
+typedef struct FsgPhantom {
+  const double* scat_xz;   /* device [n_scat*2] */
+  const double* rc;        /* device [n_scat] */
+  int64_t n_scat;
+  FsgFreqPlan plan;
+  void* out;               /* device */
+} FsgPhantom;
+
+/* Tile shapes of the batched sweep (chosen by an autotuner; zeros select defaults). */
+typedef struct FsgBatchTuning {
+  int32_t freqs_per_item;    /* 1 or 2 frequencies per work item (Green's tile reuse) */
+  int32_t chunk_scatterers;  /* scatterers per work item (rounded up to a multiple of 64) */
+  int32_t ctas_per_sm;       /* persistent CTAs per SM */
+  int32_t reserved0;
+} FsgBatchTuning;
+
+/* Workspace bytes needed by fsg_simus_batched. */
+size_t fsg_simus_batched_workspace_size(const FsgProbe* probe, const FsgPhantom* phantoms, int32_t n_phantoms,
+                                        int32_t n_tx, const FsgBatchTuning* tuning);
+
+/*
+ * Many transmits x many phantoms in one persistent launch.  Replaces the reference's caller
+ * loop of simus_compute over firings with one shared plan per phantom
+ * (tests/_picmus_phantom_shared.py:319-367, step body _simus_strategies.py:23-77): the
+ * Green's terms of each (scatterer, element, frequency) are generated once and contracted with
+ * every transmit.  delays/apod are device [n_tx][n_elements] float64 (apod NULL = ones; NaN
+ * delay = element off).  Limits of this build: n_elements <= 64, n_tx <= 80, n_phantoms <= 64.
+ * Phantom descriptors travel as a kernel parameter, so the call contains no host-to-device
+ * copy and can be captured in a CUDA graph.
+ */
+int32_t fsg_simus_batched(const FsgProbe* probe, const FsgMedium* medium, const FsgPhantom* phantoms,
+                          int32_t n_phantoms, const double* delays, const double* apod, int32_t n_tx,
+                          const FsgBatchTuning* tuning, void* workspace, size_t workspace_bytes, void* stream);
+
 /*
  * fsg_simus without a workspace argument, for callers that cannot allocate device memory
  * (for example a plugin whose host application owns all device memory and passes only input

@@ -1,0 +1,102 @@
+"""GPU parity of the batched multi-transmit / multi-phantom sweep (fsg_simus_batched)."""
+
+import numpy as np
+import pytest
+
+import oracle.fastsimus_fp64 as O
+from tests import _golden as G
+from tests._gpu import np64, require_gpu, torch
+
+pytestmark = pytest.mark.gpu
+
+PLAIN_TOL = 1e-5
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _gpu():
+    require_gpu()
+
+
+def test_batched_matches_reference_multi_firing_golden():
+    from fastsimus_gb300.batched import BatchedSimus
+
+    g = G.load("simus_multi3_cfg1")
+    b = BatchedSimus([(g.scatterers, g.rc)], g.delays, g.params, g.medium)
+    np.testing.assert_array_equal(b.plans[0].selected_freqs, g.plan_selected_freqs)
+    rf = np64(b.run()[0].rf)
+    assert rf.shape == g.rf.shape
+    err = G.rel_l2(rf, g.rf)
+    print(f"batched multi3 relL2 {err:.3e}")
+    assert err < PLAIN_TOL
+
+
+@pytest.mark.parametrize("fb", [1, 2])
+def test_batched_many_phantoms_vs_oracle(fb):
+    from fastsimus_gb300 import workloads as W
+    from fastsimus_gb300.batched import BatchedSimus, BatchTuning
+
+    p, m = W.cfg1_probe(), W.cfg1_medium()
+    rng = np.random.default_rng(11)
+    phantoms = []
+    for n, box in ((150, ((-10e-3, 10e-3), (5e-3, 30e-3))), (70, ((-4e-3, 4e-3), (4e-3, 12e-3))),
+                   (230, ((-8e-3, 6e-3), (10e-3, 35e-3)))):
+        s = W.uniform_box(rng, n, *box)
+        phantoms.append((s, rng.standard_normal(n)))
+    delays = W.plane_wave_delays(p, m, [-10.0, -3.0, 0.0, 4.0, 12.0])
+    delays[2, 5] = np.nan
+    apod = np.hanning(64) + 0.2
+    b = BatchedSimus(phantoms, delays, p, m, tx_apodization=apod, tuning=BatchTuning(fb, 64, 1))
+    res = b.run()
+    for (s, r), plan, out in zip(phantoms, b.plans, res):
+        rf = np64(out.rf)
+        for t in range(delays.shape[0]):
+            ref = O.simus_compute(s, r, delays[t], plan, p, m, tx_apodization=apod)
+            err = G.rel_l2(rf[:, :, t], ref.rf)
+            assert err < PLAIN_TOL, (t, err)
+
+
+def test_graph_replay_equals_eager_and_autotune():
+    from fastsimus_gb300 import workloads as W
+    from fastsimus_gb300.batched import BatchedSimus, BatchTuning
+
+    p, m = W.cfg1_probe(), W.cfg1_medium()
+    phantoms = [W.cfg1_scatterers(3000, seed=s) for s in (1, 2)]
+    delays = W.plane_wave_delays(p, m, np.linspace(-16, 16, 9))
+    b = BatchedSimus(phantoms, delays, p, m, tuning=BatchTuning(2, 1024, 1))
+    eager = [np64(r.rf) for r in b.run()]
+    b.capture()
+    rep = [np64(r.rf) for r in b.replay()]
+    for a, c in zip(eager, rep):
+        np.testing.assert_array_equal(a, c)
+    best = b.autotune(candidates=[BatchTuning(1, 1024, 1), BatchTuning(2, 2048, 1)], cache=False)
+    assert best in (BatchTuning(1, 1024, 1), BatchTuning(2, 2048, 1))
+    tuned = [np64(r.rf) for r in b.run()]
+    for a, c in zip(eager, tuned):
+        assert G.rel_l2(c, a) < PLAIN_TOL
+
+
+def test_batched_consistent_with_plain_kernel_at_scale():
+    """Cross-implementation property at 20k scatterers: every firing of the batched sweep
+    equals the single-transmit plain kernel run with the same plan."""
+    import fastsimus_gb300 as F
+    from fastsimus_gb300 import workloads as W
+    from fastsimus_gb300.batched import BatchedSimus
+
+    p, m = W.cfg1_probe(), W.cfg1_medium()
+    s, r = W.cfg4_scatterers(20_000, seed=5)
+    delays = W.plane_wave_delays(p, m, [-12.0, 0.0, 12.0])
+    b = BatchedSimus([(s, r)], delays, p, m)
+    spec = np64(b.run()[0].spectrum)
+    for t in range(3):
+        ref = np64(F.simus_compute(s, r, delays[t], b.plans[0], p, m).spectrum)
+        assert G.rel_l2(spec[:, :, t], ref) < PLAIN_TOL
+
+
+def test_batched_rejects_unsupported_shapes():
+    from fastsimus_gb300 import workloads as W
+    from fastsimus_gb300.batched import BatchedSimus
+
+    p2, m2 = W.cfg2_probe(), W.cfg2_medium()  # 128 elements > 64
+    s, r = W.cfg2_scatterers(100)
+    with pytest.raises(NotImplementedError):
+        BatchedSimus([(s, r)], np.zeros((2, 128)), p2, m2).run()

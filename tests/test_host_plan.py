@@ -104,3 +104,13 @@ def test_param_validation_matches_reference_rules():
     assert p.baffle is BaffleType.RIGID and p.element_width == pytest.approx(2.5e-4)
     with pytest.raises(ValueError):
         P.probe_spectrum(np.array([1.0]), 5e6, 2.0)
+
+
+def test_shared_plan_rule_matches_oracle():
+    from fastsimus_gb300.batched import shared_plan
+
+    g = G.load("simus_multi3_cfg1")
+    pl = shared_plan(g.scatterers, g.rc, list(g.delays), g.params, g.medium)
+    plo, _ = O.simus_multi_transmit(g.scatterers, g.rc, list(g.delays[:1]), g.params, g.medium)
+    np.testing.assert_array_equal(pl.selected_freqs, g.plan_selected_freqs)
+    assert pl.n_fft == int(g.plan_n_fft)
