@@ -74,6 +74,16 @@ _SIGNATURES = {
     "fsg_simus_batched": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgMedium),
                                            ctypes.POINTER(FsgPhantom), ctypes.c_int32, _P, _P, ctypes.c_int32,
                                            ctypes.POINTER(FsgBatchTuning), _P, ctypes.c_size_t, _P]),
+    "fsg_simus_batched_tc_workspace_size": (ctypes.c_size_t, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgPhantom),
+                                                              ctypes.c_int32, ctypes.c_int32,
+                                                              ctypes.POINTER(FsgBatchTuning)]),
+    "fsg_simus_batched_tc": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgMedium),
+                                              ctypes.POINTER(FsgPhantom), ctypes.c_int32, _P, _P, ctypes.c_int32,
+                                              ctypes.POINTER(FsgBatchTuning), _P, ctypes.c_size_t, _P]),
+    "fsg_simus_batched_tc_status": (ctypes.c_int32, [_P, ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgPhantom),
+                                                     ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(FsgBatchTuning),
+                                                     ctypes.POINTER(ctypes.c_int32), _P]),
+    "fsg_tc_selftest": (ctypes.c_int32, [_P, _P, _P, ctypes.c_int32, ctypes.c_int32, _P, _P]),
     "fsg_simus_noalloc": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgMedium),
                                            ctypes.POINTER(FsgFreqPlan), _P, _P, ctypes.c_int64, _P, _P, ctypes.c_int32,
                                            ctypes.c_int32, _P, _P]),

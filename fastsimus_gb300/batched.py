@@ -40,6 +40,10 @@ class BatchTuning:
     chunk_scatterers: int = 32768
     ctas_per_sm: int = 1
 
+    @staticmethod
+    def default(backend: str) -> "BatchTuning":
+        return BatchTuning(6, 65536, 1) if backend == "tc" else BatchTuning()
+
     def to_c(self) -> _native.FsgBatchTuning:
         return _native.FsgBatchTuning(self.freqs_per_item, self.chunk_scatterers, self.ctas_per_sm, 0)
 
@@ -64,7 +68,10 @@ class BatchedSimus:
 
     def __init__(self, phantoms, delays, params: TransducerParams, medium: MediumParams = _DEFAULT_MEDIUM, *,
                  plans: list[SimusPlan] | None = None, tx_apodization=None, tuning: BatchTuning | None = None,
-                 fs: float | None = None, device: torch.device | None = None):
+                 fs: float | None = None, device: torch.device | None = None, backend: str = "fp32"):
+        if backend not in ("fp32", "tc"):
+            raise ValueError("backend must be 'fp32' (CUDA cores) or 'tc' (tcgen05 BF16 hi/lo tensor cores)")
+        self.backend = backend
         self.device = device or _device.require_cuda()
         self.lib = _native.load()
         self.params, self.medium = params, medium
@@ -96,7 +103,7 @@ class BatchedSimus:
             raise ValueError("all phantoms of a batch must share n_sub")
         self.med = _native.make_medium(medium)
         self.graph = None
-        self.set_tuning(tuning or BatchTuning())
+        self.set_tuning(tuning or BatchTuning.default(backend))
 
     # -- native call -------------------------------------------------------------------------
     def _fsg_phantoms(self):
@@ -112,8 +119,9 @@ class BatchedSimus:
     def set_tuning(self, tuning: BatchTuning):
         self.tuning = tuning
         self._ph = self._fsg_phantoms()
-        nbytes = self.lib.fsg_simus_batched_workspace_size(self.probe, self._ph, len(self.phantoms), self.n_tx,
-                                                           tuning.to_c())
+        size_fn = (self.lib.fsg_simus_batched_tc_workspace_size if self.backend == "tc"
+                   else self.lib.fsg_simus_batched_workspace_size)
+        nbytes = size_fn(self.probe, self._ph, len(self.phantoms), self.n_tx, tuning.to_c())
         if nbytes == 0:
             raise ValueError("fsg_simus_batched_workspace_size rejected the batch")
         self.ws = _device.workspace(nbytes, self.device)
@@ -121,12 +129,26 @@ class BatchedSimus:
 
     def launch_sweep(self):
         """Enqueue the batched sweep on the current stream (outputs: corrected spectra)."""
+        fn = self.lib.fsg_simus_batched_tc if self.backend == "tc" else self.lib.fsg_simus_batched
         with torch.cuda.device(self.device), _device.timed("fsg_simus_batched", self.device):
-            st = self.lib.fsg_simus_batched(self.probe, self.med, self._ph, len(self.phantoms),
+            st = fn(self.probe, self.med, self._ph, len(self.phantoms),
                                             self.delays.data_ptr(), self.apod.data_ptr() if self.apod is not None
                                             else None, self.n_tx, self.tuning.to_c(), self.ws.data_ptr(),
                                             self.ws.numel(), _device.stream_handle(self.device))
         _native.check(st)
+
+    def device_status(self) -> int:
+        """Synchronise and return the device-side status of the last tensor-core sweep
+        (0 = ok, 3 = a bounded wait gave up); always 0 for the FP32 backend."""
+        if self.backend != "tc":
+            return 0
+        import ctypes
+
+        out = ctypes.c_int32(-1)
+        _native.check(self.lib.fsg_simus_batched_tc_status(self.ws.data_ptr(), self.probe, self._ph,
+                                                            len(self.phantoms), self.n_tx, self.tuning.to_c(),
+                                                            ctypes.byref(out), _device.stream_handle(self.device)))
+        return int(out.value)
 
     def _finish(self):
         self.rfs = []
@@ -179,6 +201,8 @@ class BatchedSimus:
             best = BatchTuning(**table[key])
             self.set_tuning(best)
             return best
+        if candidates is None and self.backend == "tc":
+            candidates = [BatchTuning(fb, 65536, 1) for fb in (4, 5, 6, 7)]
         if candidates is None:
             total = sum(int(s.shape[0]) for s, _ in self.phantoms)
             chunks = sorted({c for c in (8192, 16384, 32768, 65536, 131072) if c < 2 * max(total, 64)} or {8192})
@@ -206,7 +230,7 @@ class BatchedSimus:
     def _tune_key(self) -> str:
         total = sum(int(s.shape[0]) for s, _ in self.phantoms)
         fbar = int(np.mean([p.selected_freqs.shape[0] for p in self.plans]))
-        return (f"E{self.params.n_elements}-U{self.plans[0].n_sub}-T{self.n_tx}-P{len(self.phantoms)}"
+        return (f"{self.backend}-E{self.params.n_elements}-U{self.plans[0].n_sub}-T{self.n_tx}-P{len(self.phantoms)}"
                 f"-S{int(np.log2(max(total, 1)))}-F{fbar // 64}")
 
 
@@ -242,9 +266,9 @@ def _save_cache(table: dict):
 
 def simus_batched(phantoms, delays, params: TransducerParams, medium: MediumParams = _DEFAULT_MEDIUM, *,
                   plans: list[SimusPlan] | None = None, tx_apodization=None, fs: float | None = None,
-                  tuning: BatchTuning | None = None) -> list[SimusResult]:
+                  tuning: BatchTuning | None = None, backend: str = "fp32") -> list[SimusResult]:
     """RF of every (phantom, firing): ``phantoms`` is a list of (scatterers (S, 2), rc (S,)),
     ``delays`` is (n_tx, n_elements).  Returns per phantom rf (n_samples, E, n_tx) float32 and
     spectrum (n_freq_full, E, n_tx) complex64, on the GPU."""
     return BatchedSimus(phantoms, delays, params, medium, plans=plans, tx_apodization=tx_apodization,
-                        tuning=tuning, fs=fs).run()
+                        tuning=tuning, fs=fs, backend=backend).run()

@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "../../include/fsgb300.h"
 #include "fsg_batched.h"
@@ -260,7 +261,7 @@ __global__ void batched_reduce(const __grid_constant__ BatchReduceArgs a) {
       const int band = f / a.fb, fl = f % a.fb;
       for (int c = 0; c < P.n_chunks; ++c) {
         const int item = P.item0 + c * P.n_bands + band;
-        acc = cadd(acc, a.partial[(((size_t)item * a.fb + fl) * kBTX + t) * kBE + e]);
+        acc = cadd(acc, a.partial[(((size_t)item * a.fb + fl) * a.tx_pad + t) * a.e_pad + e]);
       }
       const float s = P.probe[f] * P.corr;
       acc = make_float2(acc.x * s, acc.y * s);
@@ -497,6 +498,8 @@ extern "C" int32_t fsg_simus_batched(const FsgProbe* probe, const FsgMedium* med
     a.n_tx = n_tx;
     a.E = E;
     a.fb = L.fb;
+    a.tx_pad = kBTX;
+    a.e_pad = kBE;
     a.partial = partial;
     batched_reduce<<<dim3(2 * sms, n_phantoms), 256, 0, s>>>(a);
     if ((st = check_cuda(cudaGetLastError(), "batched_reduce launch")) != FSG_OK) return st;

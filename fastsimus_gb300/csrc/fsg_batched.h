@@ -58,6 +58,7 @@ struct BatchSetupArgs {
 struct BatchReduceArgs {
   BatchPhantom ph[kMaxPhantoms];
   int n_phantoms, n_tx, E, fb;
+  int tx_pad, e_pad;        // partial layout [item][fb][tx_pad][e_pad]
   const float2* partial;
 };
 

@@ -1,0 +1,683 @@
+// Tensor-core (tcgen05) multi-transmit simus sweep: Green's tiles generated on chip in FP32,
+// split into BF16 hi + lo, three-product complex GEMMs with FP32 accumulation in TMEM.
+//
+// Work item = (phantom, band of `fb` consecutive frequencies, scatterer chunk); one CTA of 256
+// threads per SM pulls items from an atomic counter.  Per tile of 64 scatterers and frequency f:
+//
+//   generate   Gm[s][e] = mean_u G(s, e, u, f)            (FP32 recurrence, 32 states / thread)
+//   TX  (MMA)  D_tx[(c,s)][(c',t)] = sum_e Gc[s][e] * Dc'[e][t]     M=128 N=64 K=64
+//              with c, c' in {re, im}: rows [Gr; Gi], columns [Dr | Di]
+//              P = (D_tx[0,s][0,t] - D_tx[1,s][1,t]) + i (D_tx[0,s][1,t] + D_tx[1,s][0,t])
+//   RX  (MMA)  D_rx[f][(c,e)][(c',t)] += sum_s Wc[s][e] * Pc'[s][t]  M=128 N=64 K=64
+//              with W = Gm * rc_s * pulse * probe (rows [Wr^T; Wi^T]) and columns [Pr | Pi];
+//              Y = D_rx[0][0] - D_rx[1][1] + i (D_rx[0][1] + D_rx[1][0]) is formed once per item.
+//
+// Each real GEMM is A_hi B_hi + A_hi B_lo + A_lo B_hi (three tcgen05.mma kind::f16 per K step).
+// TX operands are K-major; RX operands are written MN-major so that no thread transposes data.
+// Every wait on an mbarrier is bounded: on timeout the CTA records FSG_ETIMEOUT in the status
+// word, skips the remaining work, frees its TMEM and exits.
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "../../include/fsgb300.h"
+#include "fsg_batched.h"
+#include "fsg_common.cuh"
+#include "fsg_internal.h"
+#include "fsg_tc.cuh"
+
+namespace fsg {
+
+constexpr int kTcT = 64;        // scatterers per tile
+constexpr int kTcE = 64;        // padded elements
+constexpr int kTcTx = 32;       // padded transmits
+constexpr int kTcMaxFb = 7;     // TMEM: 64 (TX) + 64 per band frequency <= 512 columns
+constexpr uint32_t kTmemCols = 512;
+constexpr uint32_t kWaitTries = 1u << 26;
+
+struct TcArgs {
+  BatchPhantom ph[kMaxPhantoms];
+  int n_phantoms, n_items, E, U, n_tx, fb, convex;
+  int64_t chunk;
+  const float4* src_pos;
+  const float2* rot_e;
+  const float2* tau;
+  const float* apod;
+  SweepConst C;
+  double apex, radius2;
+  int* queue;
+  int* status;
+  float2* partial;  // [n_items][fb][kTcTx][kTcE]
+};
+
+// Geometry for the tensor-core path: same distance / amplitude / anchor as the plain kernels;
+// the recurrence step comes from the MUFU sin/cos (its ~4e-7 error compounds over < 7 steps).
+__device__ __forceinline__ void tc_source(dfl xs, dfl zs, float4 sp, float2 rot, const SweepConst& C, float2 k0,
+                                          float a0, float2& g, float2& st) {
+  const SrcGeo geo = source_geometry(xs, zs, sp, rot, C);
+  g = anchor_value(geo.r_hi, geo.r_lo, geo.amp, k0, a0);
+  st = geo.step;
+}
+
+// SMEM layout (bytes).
+constexpr uint32_t kOffAtxHi = 0;                 // K-major  128 x 64 bf16
+constexpr uint32_t kOffAtxLo = 16384;
+constexpr uint32_t kOffArxHi = 32768;             // MN-major 128 x 64 bf16
+constexpr uint32_t kOffArxLo = 49152;
+constexpr uint32_t kOffBrxHi = 65536;             // MN-major 64 (n) x 64 (k)
+constexpr uint32_t kOffBrxLo = 73728;
+constexpr uint32_t kOffX = 81920;                 // exchange: 2 x 64 x 32 floats
+constexpr uint32_t kOffBtx = 98304;               // per band frequency: K-major 64 x 64, hi then lo
+constexpr uint32_t kBtxBytes = 16384;
+
+__host__ __device__ constexpr uint32_t tc_smem_bytes(int fb) { return kOffBtx + (uint32_t)fb * kBtxBytes + 1024; }
+
+template <int U>
+__global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__ TcArgs A) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ uint64_t mbar_tx, mbar_rx;
+  __shared__ uint32_t tmem_holder;
+  __shared__ int s_item, s_fail;
+  __shared__ float rcs[kTcT];
+  __shared__ float2 pps[kTcMaxFb];
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int fb = A.fb, E = A.E, T = A.n_tx;
+  if (tid == 0) {
+    tc::mbar_init(&mbar_tx, 1);
+    tc::mbar_init(&mbar_rx, 1);
+    tc::fence_mbar_init();
+    s_fail = 0;
+  }
+  if (warp == 0) tc::tmem_alloc(&tmem_holder, kTmemCols);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_holder;
+  // mbarrier phases and the pending-RX flag are only used by thread 0
+  uint32_t ph_tx = 0, ph_rx = 0;
+  bool rx_pending = false;
+
+  const uint32_t sbase = tc::smem_u32(sm);
+  const uint32_t id_tx = tc::idesc_bf16(128, 64, 0, 0);  // A K-major, B K-major
+  const uint32_t id_rx = tc::idesc_bf16(128, 64, 1, 1);  // A MN-major, B MN-major
+  float* X = reinterpret_cast<float*>(sm + kOffX);
+  float4* stage = reinterpret_cast<float4*>(sm + kOffAtxHi);  // geometry staging (A_tx region)
+
+  // generation mapping: scatterer s_g of the tile, elements [16 eg, 16 eg + 16)
+  const int s_g = tid >> 2, eg = tid & 3;
+  // TMEM read mapping: lane quarter q (rows 32q..32q+31), column half h
+  const int q = warp & 3, h = warp >> 2;
+
+  // thread 0 waits on an mbarrier (bounded); the result reaches every thread through s_fail
+  // after the next __syncthreads, so all threads take the same branches.
+  auto wait0 = [&](uint64_t* mb, uint32_t& ph) {
+    if (tid == 0) {
+      if (!tc::mbar_wait_bounded(mb, ph, kWaitTries)) s_fail = 1;
+      ph ^= 1u;
+    }
+  };
+
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) s_item = s_fail ? A.n_items : atomicAdd(A.queue, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= A.n_items) break;
+    int p = 0;
+    while (p + 1 < A.n_phantoms && item >= A.ph[p + 1].item0) ++p;
+    const BatchPhantom& P = A.ph[p];
+    const int local = item - P.item0;
+    const int band = local % P.n_bands, chunk = local / P.n_bands;
+    const int f0 = band * fb;
+    const int nf = min(fb, P.n_freq - f0);
+    const int64_t s_begin = (int64_t)chunk * A.chunk;
+    const int64_t s_end = min(P.n_scat, s_begin + A.chunk);
+    SweepConst C = A.C;
+    C.dk = P.dk;
+    C.dalpha = P.dalpha;
+
+    // ---- B_tx for the band: K-major rows n' = (c', t), K = e; value D_c'(e, t) ----
+    for (int i = tid; i < fb * 64 * 64; i += kThreads) {
+      const int f = i >> 12, n = (i >> 6) & 63, e = i & 63;
+      const int c = n >> 5, t = n & 31;
+      float v = 0.f;
+      if (f < nf && e < E && t < T) {
+        const float w = A.apod[t * E + e];
+        if (w != 0.f) {
+          const float2 tau = A.tau[t * E + e];
+          const float2 fr = P.freq_hz[f0 + f];
+          const float pr = __fmul_rn(fr.x, tau.x);
+          float er = fmaf(fr.x, tau.x, -pr);
+          er = fmaf(fr.x, tau.y, er);
+          er = fmaf(fr.y, tau.x, er);
+          const float x = __fadd_rn(__fsub_rn(pr, rintf(pr)), er);  // cycles, |x| <= 0.5
+          float sn, cs;
+          sincospif(2.0f * x, &sn, &cs);
+          v = w * (c ? sn : cs);
+        }
+      }
+      __nv_bfloat16 hi, lo;
+      tc::split_bf16(v, hi, lo);
+      unsigned char* bt = sm + kOffBtx + f * kBtxBytes;
+      const uint32_t off = tc::kmajor_off(n, e, 8);
+      *reinterpret_cast<__nv_bfloat16*>(bt + off) = hi;
+      *reinterpret_cast<__nv_bfloat16*>(bt + 8192 + off) = lo;
+    }
+    if (tid < kTcMaxFb) pps[tid] = (tid < nf) ? P.pp[f0 + tid] : make_float2(0.f, 0.f);
+    const float2 k0 = P.kf[f0];
+    const float a0 = P.af[f0];
+    bool first_tile = true;
+
+    for (int64_t t0 = s_begin; t0 < s_end; t0 += kTcT) {
+      const int64_t s = t0 + s_g;
+      const bool sval = s < s_end;
+      if (eg == 0) {
+        float w = 0.f;
+        if (sval) {
+          const double x = P.scat[2 * s], z = P.scat[2 * s + 1];
+          bool out = z < 0.0;
+          if (A.convex) out = out || (x * x + (z + A.apex) * (z + A.apex) <= A.radius2);
+          w = out ? 0.f : (float)P.rc[s];
+        }
+        rcs[s_g] = w;
+      }
+      // ---- geometry of 16 elements x U sub-elements, 8 states at a time through shared memory ----
+      float2 G[16 * U], S[16 * U];
+      {
+        const int64_t si = sval ? s : t0;
+        const dfl xs = split_double(P.scat[2 * si]);
+        const dfl zs = split_double(P.scat[2 * si + 1]);
+#pragma unroll
+        for (int c = 0; c < 2 * U; ++c) {
+#pragma unroll 1
+          for (int i = 0; i < 8; ++i) {
+            const int idx = c * 8 + i;  // state index j * U + u
+            const int e = eg * 16 + idx / U, u = idx % U;
+            float2 g = make_float2(0.f, 0.f), st = make_float2(0.f, 0.f);
+            if (sval && e < E) tc_source(xs, zs, A.src_pos[e * U + u], A.rot_e[e], C, k0, a0, g, st);
+            stage[tid * 8 + i] = make_float4(g.x, g.y, st.x, st.y);
+          }
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const float4 v = stage[tid * 8 + i];
+            G[c * 8 + i] = make_float2(v.x, v.y);
+            S[c * 8 + i] = make_float2(v.z, v.w);
+          }
+        }
+      }
+      __syncthreads();  // staging area (A_tx region) is reused below; rcs visible
+      const float rc_s = rcs[s_g];
+
+      for (int f = 0; f < nf; ++f) {
+        // previous RX MMAs read A_rx / B_rx: wait before overwriting
+        if (tid == 0 && rx_pending) {
+          wait0(&mbar_rx, ph_rx);
+          rx_pending = false;
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (s_fail) break;
+        const float2 sc = make_float2(rc_s * pps[f].x, rc_s * pps[f].y);
+        // ---- Green's values at f; write A_tx (K-major rows (c, s), K = e) and
+        //      A_rx (MN-major rows (c, e), K = s) in halves of 8 elements ----
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+          float gr[8], gi[8], wr[8], wi[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int jj = half * 8 + j;
+            float2 acc = G[jj * U];
+#pragma unroll
+            for (int u = 1; u < U; ++u) acc = cadd(acc, G[jj * U + u]);
+            gr[j] = acc.x;
+            gi[j] = acc.y;
+            wr[j] = acc.x * sc.x - acc.y * sc.y;
+            wi[j] = acc.x * sc.y + acc.y * sc.x;
+#pragma unroll
+            for (int u = 0; u < U; ++u) G[jj * U + u] = cmul(G[jj * U + u], S[jj * U + u]);
+          }
+          const int e0 = eg * 16 + half * 8;
+          uint4 hr, lr, hi_, li_;
+          tc::split8(gr, hr, lr);
+          tc::split8(gi, hi_, li_);
+          const uint32_t o_re = tc::kmajor_off(s_g, e0, 8), o_im = tc::kmajor_off(64 + s_g, e0, 8);
+          *reinterpret_cast<uint4*>(sm + kOffAtxHi + o_re) = hr;
+          *reinterpret_cast<uint4*>(sm + kOffAtxLo + o_re) = lr;
+          *reinterpret_cast<uint4*>(sm + kOffAtxHi + o_im) = hi_;
+          *reinterpret_cast<uint4*>(sm + kOffAtxLo + o_im) = li_;
+          tc::split8(wr, hr, lr);
+          tc::split8(wi, hi_, li_);
+          const uint32_t q_re = tc::mnmajor_off(e0, s_g, 16), q_im = tc::mnmajor_off(64 + e0, s_g, 16);
+          *reinterpret_cast<uint4*>(sm + kOffArxHi + q_re) = hr;
+          *reinterpret_cast<uint4*>(sm + kOffArxLo + q_re) = lr;
+          *reinterpret_cast<uint4*>(sm + kOffArxHi + q_im) = hi_;
+          *reinterpret_cast<uint4*>(sm + kOffArxLo + q_im) = li_;
+        }
+        tc::fence_proxy_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        // ---- TX MMAs ----
+        if (tid == 0) {
+          const uint32_t bt = sbase + kOffBtx + f * kBtxBytes;
+#pragma unroll
+          for (int ks = 0; ks < 4; ++ks) {
+            const uint64_t ah = tc::sdesc(sbase + kOffAtxHi + ks * 256, 128, 1024);
+            const uint64_t al = tc::sdesc(sbase + kOffAtxLo + ks * 256, 128, 1024);
+            const uint64_t bh = tc::sdesc(bt + ks * 256, 128, 1024);
+            const uint64_t bl = tc::sdesc(bt + 8192 + ks * 256, 128, 1024);
+            tc::mma_bf16(tmem, ah, bh, id_tx, ks > 0);
+            tc::mma_bf16(tmem, ah, bl, id_tx, 1);
+            tc::mma_bf16(tmem, al, bh, id_tx, 1);
+          }
+          tc::commit(&mbar_tx);
+          wait0(&mbar_tx, ph_tx);
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (s_fail) break;
+        // ---- P = combine(D_tx); write B_rx (MN-major rows n' = (c', t), K = s) ----
+        float v[32];
+        tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + 32 * h, v);
+        const int row = 32 * q + lane;  // (c, s) with c = row / 64
+        if (row >= 64) {
+#pragma unroll
+          for (int t = 0; t < 32; ++t) X[(h * 64 + (row - 64)) * 32 + t] = v[t];
+        }
+        __syncthreads();
+        if (row < 64) {
+          // h = 0: Pr = D[0,s][0,t] - D[1,s][1,t];  h = 1: Pi = D[0,s][1,t] + D[1,s][0,t]
+          const float* x = X + ((1 - h) * 64 + row) * 32;
+#pragma unroll
+          for (int t = 0; t < 32; ++t) v[t] = h ? v[t] + x[t] : v[t] - x[t];
+#pragma unroll
+          for (int c8 = 0; c8 < 4; ++c8) {
+            uint4 hh, ll;
+            tc::split8(v + 8 * c8, hh, ll);
+            const uint32_t o = tc::mnmajor_off(32 * h + 8 * c8, row, 8);
+            *reinterpret_cast<uint4*>(sm + kOffBrxHi + o) = hh;
+            *reinterpret_cast<uint4*>(sm + kOffBrxLo + o) = ll;
+          }
+        }
+        tc::fence_proxy_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        // ---- RX MMAs into this frequency's accumulator ----
+        if (tid == 0) {
+          const uint32_t d = tmem + 64 + 64 * f;
+#pragma unroll
+          for (int ks = 0; ks < 4; ++ks) {
+            const uint64_t ah = tc::sdesc(sbase + kOffArxHi + ks * 2 * 2048, 2048, 128);
+            const uint64_t al = tc::sdesc(sbase + kOffArxLo + ks * 2 * 2048, 2048, 128);
+            const uint64_t bh = tc::sdesc(sbase + kOffBrxHi + ks * 2 * 1024, 1024, 128);
+            const uint64_t bl = tc::sdesc(sbase + kOffBrxLo + ks * 2 * 1024, 1024, 128);
+            tc::mma_bf16(d, ah, bh, id_rx, (first_tile && ks == 0) ? 0u : 1u);
+            tc::mma_bf16(d, ah, bl, id_rx, 1);
+            tc::mma_bf16(d, al, bh, id_rx, 1);
+          }
+          tc::commit(&mbar_rx);
+          rx_pending = true;
+        }
+      }
+      first_tile = false;
+      __syncthreads();
+      if (s_fail) break;
+    }
+    // ---- drain, then Y = combine(D_rx[f]) -> partial[item][f][t][e] ----
+    if (tid == 0 && rx_pending) {
+      wait0(&mbar_rx, ph_rx);
+      rx_pending = false;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const bool fail = s_fail != 0;
+    float2* out = A.partial + (size_t)item * fb * kTcTx * kTcE;
+    for (int f = 0; f < fb; ++f) {
+      float v[32];
+      const bool have = !first_tile && f < nf && !fail;
+      if (have) tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + 64 + 64 * f + 32 * h, v);
+      const int row = 32 * q + lane;  // (c, e)
+      if (row >= 64) {
+#pragma unroll
+        for (int t = 0; t < 32; ++t) X[(h * 64 + (row - 64)) * 32 + t] = have ? v[t] : 0.f;
+      }
+      __syncthreads();
+      if (row < 64) {
+        const float* x = X + ((1 - h) * 64 + row) * 32;
+#pragma unroll
+        for (int t = 0; t < 32; ++t) {
+          const float val = have ? (h ? v[t] + x[t] : v[t] - x[t]) : 0.f;
+          float* o = reinterpret_cast<float*>(out + ((size_t)f * kTcTx + t) * kTcE + row);
+          o[h] = val;  // h = 0 real part, h = 1 imaginary part
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // ---- release TMEM ----
+  tc::fence_before_sync();
+  __syncthreads();
+  if (s_fail && tid == 0) atomicExch(A.status, FSG_ETIMEOUT);
+  if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+}
+
+// Single-tile check of the tcgen05 GEMM building block: D (128 x 64) = A (128 x 64) B^T, with
+// A and B given row-major in FP32, split into BF16 hi/lo and laid out K-major or MN-major.
+__global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const float* Ag, const float* Bg, float* Dg, int a_mn,
+                                                              int b_mn, int* status) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t tmem_holder;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    tc::mbar_init(&mbar, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) tc::tmem_alloc(&tmem_holder, 64);
+  // A: 32 KB region (hi at 0, lo at 16384); B: hi at 32768, lo at 40960
+  for (int k = 0; k < 64; ++k) {
+    __nv_bfloat16 hi, lo;
+    tc::split_bf16(Ag[tid * 64 + k], hi, lo);
+    const uint32_t o = a_mn ? tc::mnmajor_off(tid, k, 16) : tc::kmajor_off(tid, k, 8);
+    *reinterpret_cast<__nv_bfloat16*>(sm + o) = hi;
+    *reinterpret_cast<__nv_bfloat16*>(sm + 16384 + o) = lo;
+    if (tid < 64) {
+      tc::split_bf16(Bg[tid * 64 + k], hi, lo);
+      const uint32_t ob = b_mn ? tc::mnmajor_off(tid, k, 8) : tc::kmajor_off(tid, k, 8);
+      *reinterpret_cast<__nv_bfloat16*>(sm + 32768 + ob) = hi;
+      *reinterpret_cast<__nv_bfloat16*>(sm + 40960 + ob) = lo;
+    }
+  }
+  tc::fence_proxy_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_holder;
+  const uint32_t sb = tc::smem_u32(sm);
+  if (tid == 0) {
+    const uint32_t idesc = tc::idesc_bf16(128, 64, a_mn, b_mn);
+    for (int ks = 0; ks < 4; ++ks) {
+      uint64_t ah, al, bh, bl;
+      if (a_mn) {
+        ah = tc::sdesc(sb + ks * 2 * 2048, 2048, 128);
+        al = tc::sdesc(sb + 16384 + ks * 2 * 2048, 2048, 128);
+      } else {
+        ah = tc::sdesc(sb + ks * 256, 128, 1024);
+        al = tc::sdesc(sb + 16384 + ks * 256, 128, 1024);
+      }
+      if (b_mn) {
+        bh = tc::sdesc(sb + 32768 + ks * 2 * 1024, 1024, 128);
+        bl = tc::sdesc(sb + 40960 + ks * 2 * 1024, 1024, 128);
+      } else {
+        bh = tc::sdesc(sb + 32768 + ks * 256, 128, 1024);
+        bl = tc::sdesc(sb + 40960 + ks * 256, 128, 1024);
+      }
+      tc::mma_bf16(tmem, ah, bh, idesc, ks > 0);
+      tc::mma_bf16(tmem, ah, bl, idesc, 1);
+      tc::mma_bf16(tmem, al, bh, idesc, 1);
+    }
+    tc::commit(&mbar);
+  }
+  const bool ok = tc::mbar_wait_bounded(&mbar, 0, kWaitTries);
+  tc::fence_after_sync();
+  float v[32];
+  if (ok) {
+    tc::tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16), v);
+    for (int j = 0; j < 32; ++j) Dg[(32 * warp + lane) * 64 + j] = v[j];
+    tc::tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + 32, v);
+    for (int j = 0; j < 32; ++j) Dg[(32 * warp + lane) * 64 + 32 + j] = v[j];
+  } else if (tid == 0) {
+    atomicExch(status, FSG_ETIMEOUT);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+}
+
+cudaError_t launch_tc(int U, int grid, const TcArgs& A, cudaStream_t s) {
+  const uint32_t smem = tc_smem_bytes(A.fb);
+  cudaError_t e;
+  if (U == 1) {
+    e = cudaFuncSetAttribute(tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    tc_kernel<1><<<grid, kThreads, smem, s>>>(A);
+  } else {
+    e = cudaFuncSetAttribute(tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    tc_kernel<2><<<grid, kThreads, smem, s>>>(A);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace fsg
+
+// ------------------------------------------------------------------------------------------
+// C ABI
+// ------------------------------------------------------------------------------------------
+
+namespace {
+
+using namespace fsg;
+
+size_t tc_a256(size_t v) { return (v + 255) & ~size_t(255); }
+
+struct TcLayout {
+  int fb, chunk, n_items;
+  int n_bands[kMaxPhantoms], n_chunks[kMaxPhantoms], item0[kMaxPhantoms];
+  size_t off_src, off_rot, off_tau, off_apod, off_queue, off_tab[kMaxPhantoms], off_partial, total;
+};
+
+void tc_layout(const FsgProbe* probe, const FsgPhantom* ph, int n_ph, int n_tx, const FsgBatchTuning* tu,
+               TcLayout* L) {
+  int fb = (tu && tu->freqs_per_item > 0) ? tu->freqs_per_item : 6;
+  if (fb > kTcMaxFb) fb = kTcMaxFb;
+  L->fb = fb;
+  int64_t chunk = (tu && tu->chunk_scatterers > 0) ? tu->chunk_scatterers : 65536;
+  chunk = ((chunk + kTcT - 1) / kTcT) * kTcT;
+  L->chunk = (int)chunk;
+  const int E = probe->n_elements, U = probe->n_sub;
+  size_t o = 0;
+  L->off_src = o; o += tc_a256((size_t)E * U * 16);
+  L->off_rot = o; o += tc_a256((size_t)E * 8);
+  L->off_tau = o; o += tc_a256((size_t)n_tx * E * 8);
+  L->off_apod = o; o += tc_a256((size_t)n_tx * E * 4);
+  L->off_queue = o; o += 256;  // queue counter + status word
+  int items = 0;
+  for (int p = 0; p < n_ph; ++p) {
+    const int F = ph[p].plan.n_freq;
+    L->n_bands[p] = (F + fb - 1) / fb;
+    L->n_chunks[p] = ph[p].n_scat > 0 ? (int)((ph[p].n_scat + chunk - 1) / chunk) : 1;
+    L->item0[p] = items;
+    items += L->n_bands[p] * L->n_chunks[p];
+    L->off_tab[p] = o;
+    o += tc_a256((size_t)F * (8 + 4 + 8 + 8 + 4));
+  }
+  L->n_items = items;
+  L->off_partial = o;
+  o += tc_a256((size_t)items * fb * kTcTx * kTcE * 8);
+  L->total = o;
+}
+
+}  // namespace
+
+extern "C" size_t fsg_simus_batched_tc_workspace_size(const FsgProbe* probe, const FsgPhantom* phantoms,
+                                                      int32_t n_phantoms, int32_t n_tx,
+                                                      const FsgBatchTuning* tuning) {
+  if (!probe || !phantoms || n_phantoms < 1 || n_phantoms > kMaxPhantoms || n_tx < 1) return 0;
+  TcLayout L;
+  tc_layout(probe, phantoms, n_phantoms, n_tx, tuning, &L);
+  return L.total;
+}
+
+extern "C" int32_t fsg_simus_batched_tc(const FsgProbe* probe, const FsgMedium* medium, const FsgPhantom* phantoms,
+                                        int32_t n_phantoms, const double* delays, const double* apod, int32_t n_tx,
+                                        const FsgBatchTuning* tuning, void* workspace, size_t workspace_bytes,
+                                        void* stream_ptr) {
+  if (!probe || !medium || !phantoms || !delays) return set_error(FSG_EINVAL, "NULL argument");
+  if (n_phantoms < 1 || n_phantoms > kMaxPhantoms) return set_error(FSG_EINVAL, "n_phantoms must be in [1, %d]", kMaxPhantoms);
+  if (n_tx < 1 || n_tx > kTcTx) return set_error(FSG_EUNSUPPORTED, "tensor-core sweep supports n_tx <= %d", kTcTx);
+  if (probe->n_elements < 1 || probe->n_elements > kTcE)
+    return set_error(FSG_EUNSUPPORTED, "tensor-core sweep supports n_elements <= %d", kTcE);
+  if (probe->n_sub < 1 || probe->n_sub > 2) return set_error(FSG_EUNSUPPORTED, "tensor-core sweep supports n_sub <= 2");
+  if (!(medium->speed_of_sound > 0) || !(medium->attenuation >= 0)) return set_error(FSG_EINVAL, "bad medium");
+  for (int p = 0; p < n_phantoms; ++p) {
+    const FsgFreqPlan& pl = phantoms[p].plan;
+    if (phantoms[p].n_scat < 0 || (phantoms[p].n_scat > 0 && (!phantoms[p].scat_xz || !phantoms[p].rc)) ||
+        !phantoms[p].out)
+      return set_error(FSG_EINVAL, "phantom %d: bad inputs", p);
+    if (pl.n_freq < 1 || !pl.pulse_spectrum || !pl.probe_spectrum || pl.freq_idx_start < 0 ||
+        pl.freq_idx_start + pl.n_freq > pl.n_freq_full)
+      return set_error(FSG_EINVAL, "phantom %d: bad plan", p);
+  }
+  TcLayout L;
+  tc_layout(probe, phantoms, n_phantoms, n_tx, tuning, &L);
+  if (!workspace || workspace_bytes < L.total)
+    return set_error(FSG_EWORKSPACE, "workspace of %zu bytes is smaller than the %zu bytes required", workspace_bytes,
+                     L.total);
+  int sms = 0, dev = 0;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (ce != cudaSuccess) return check_cuda(ce, "device query");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream_ptr);
+  unsigned char* ws = static_cast<unsigned char*>(workspace);
+  const int E = probe->n_elements, U = probe->n_sub;
+  int st;
+  {
+    SetupArgs a;
+    memset(&a, 0, sizeof(a));
+    a.E = E;
+    a.U = U;
+    a.pitch = probe->pitch;
+    a.width = probe->element_width;
+    a.radius = probe->radius;
+    a.c = medium->speed_of_sound;
+    a.seg = probe->element_width / U;
+    a.delays = delays;
+    a.t.src_pos = reinterpret_cast<float4*>(ws + L.off_src);
+    a.t.rot_e = reinterpret_cast<float2*>(ws + L.off_rot);
+    setup_tables<<<(E * U + 127) / 128, 128, 0, s>>>(a);
+    if ((st = check_cuda(cudaGetLastError(), "setup_tables launch")) != FSG_OK) return st;
+  }
+  BatchPhantom bp[kMaxPhantoms];
+  memset(bp, 0, sizeof(bp));
+  int max_f = 0;
+  for (int p = 0; p < n_phantoms; ++p) {
+    const FsgPhantom& q = phantoms[p];
+    BatchPhantom& b = bp[p];
+    b.scat = q.scat_xz;
+    b.rc = q.rc;
+    b.n_scat = q.n_scat;
+    b.n_freq = q.plan.n_freq;
+    b.n_freq_full = q.plan.n_freq_full;
+    b.freq_idx_start = q.plan.freq_idx_start;
+    b.n_bands = L.n_bands[p];
+    b.n_chunks = L.n_chunks[p];
+    b.item0 = L.item0[p];
+    b.f0 = q.plan.freq_start;
+    b.df = q.plan.freq_step;
+    b.corr = (float)q.plan.correction_factor;
+    const SweepConst cp = make_sweep_const(probe, medium, &q.plan, 0);
+    b.dk = cp.dk;
+    b.dalpha = cp.dalpha;
+    b.pulse_src = q.plan.pulse_spectrum;
+    b.probe_src = q.plan.probe_spectrum;
+    unsigned char* tb = ws + L.off_tab[p];
+    const int F = q.plan.n_freq;
+    b.kf = reinterpret_cast<float2*>(tb);
+    b.freq_hz = reinterpret_cast<float2*>(tb + (size_t)F * 8);
+    b.pp = reinterpret_cast<float2*>(tb + (size_t)F * 16);
+    b.af = reinterpret_cast<float*>(tb + (size_t)F * 24);
+    b.probe = reinterpret_cast<float*>(tb + (size_t)F * 28);
+    b.out = static_cast<float2*>(q.out);
+    if (F > max_f) max_f = F;
+  }
+  float2* tau = reinterpret_cast<float2*>(ws + L.off_tau);
+  float* apw = reinterpret_cast<float*>(ws + L.off_apod);
+  {
+    BatchSetupArgs a;
+    memcpy(a.ph, bp, sizeof(bp));
+    a.n_phantoms = n_phantoms;
+    a.n_tx = n_tx;
+    a.E = E;
+    a.c = medium->speed_of_sound;
+    a.att = medium->attenuation;
+    a.delays = delays;
+    a.apod_src = apod;
+    a.tau = tau;
+    a.apod = apw;
+    const int n = max_f > n_tx * E ? max_f : n_tx * E;
+    batched_setup<<<dim3((n + 127) / 128, n_phantoms), 128, 0, s>>>(a);
+    if ((st = check_cuda(cudaGetLastError(), "batched_setup launch")) != FSG_OK) return st;
+  }
+  int* queue = reinterpret_cast<int*>(ws + L.off_queue);
+  if ((st = check_cuda(cudaMemsetAsync(queue, 0, 2 * sizeof(int), s), "queue reset")) != FSG_OK) return st;
+  float2* partial = reinterpret_cast<float2*>(ws + L.off_partial);
+  {
+    TcArgs A;
+    memcpy(A.ph, bp, sizeof(bp));
+    A.n_phantoms = n_phantoms;
+    A.n_items = L.n_items;
+    A.E = E;
+    A.U = U;
+    A.n_tx = n_tx;
+    A.fb = L.fb;
+    A.chunk = L.chunk;
+    A.src_pos = reinterpret_cast<const float4*>(ws + L.off_src);
+    A.rot_e = reinterpret_cast<const float2*>(ws + L.off_rot);
+    A.tau = tau;
+    A.apod = apw;
+    A.C = make_sweep_const(probe, medium, &phantoms[0].plan, 0);
+    convex_geometry(probe, &A.convex, &A.apex, &A.radius2);
+    A.queue = queue;
+    A.status = queue + 1;
+    A.partial = partial;
+    int grid = sms;
+    if (grid > L.n_items) grid = L.n_items;
+    if ((st = check_cuda(launch_tc(U, grid, A, s), "tc_kernel launch")) != FSG_OK) return st;
+  }
+  {
+    BatchReduceArgs a;
+    memcpy(a.ph, bp, sizeof(bp));
+    a.n_phantoms = n_phantoms;
+    a.n_tx = n_tx;
+    a.E = E;
+    a.fb = L.fb;
+    a.tx_pad = kTcTx;
+    a.e_pad = kTcE;
+    a.partial = partial;
+    batched_reduce<<<dim3(2 * sms, n_phantoms), 256, 0, s>>>(a);
+    if ((st = check_cuda(cudaGetLastError(), "batched_reduce launch")) != FSG_OK) return st;
+  }
+  return FSG_OK;
+}
+
+extern "C" int32_t fsg_simus_batched_tc_status(const void* workspace, const FsgProbe* probe,
+                                               const FsgPhantom* phantoms, int32_t n_phantoms, int32_t n_tx,
+                                               const FsgBatchTuning* tuning, int32_t* status_out, void* stream) {
+  if (!workspace || !probe || !phantoms || !status_out) return set_error(FSG_EINVAL, "NULL argument");
+  TcLayout L;
+  tc_layout(probe, phantoms, n_phantoms, n_tx, tuning, &L);
+  const int* dev_status = reinterpret_cast<const int*>(static_cast<const unsigned char*>(workspace) + L.off_queue) + 1;
+  cudaError_t e = cudaMemcpyAsync(status_out, dev_status, sizeof(int), cudaMemcpyDeviceToHost,
+                                  reinterpret_cast<cudaStream_t>(stream));
+  if (e == cudaSuccess) e = cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream));
+  return check_cuda(e, "status read");
+}
+
+extern "C" int32_t fsg_tc_selftest(const float* a, const float* b, float* d, int32_t a_mn_major, int32_t b_mn_major,
+                                   int32_t* status, void* stream) {
+  if (!a || !b || !d || !status) return set_error(FSG_EINVAL, "NULL argument");
+  const int smem = 96 * 1024;
+  cudaError_t e = cudaFuncSetAttribute(tc_selftest_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(tc_selftest_kernel)");
+  tc_selftest_kernel<<<1, 128, smem, reinterpret_cast<cudaStream_t>(stream)>>>(a, b, d, a_mn_major, b_mn_major, status);
+  return check_cuda(cudaGetLastError(), "tc_selftest launch");
+}

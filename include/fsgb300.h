@@ -168,6 +168,37 @@ int32_t fsg_simus_batched(const FsgProbe* probe, const FsgMedium* medium, const 
                           int32_t n_phantoms, const double* delays, const double* apod, int32_t n_tx,
                           const FsgBatchTuning* tuning, void* workspace, size_t workspace_bytes, void* stream);
 
+/* Workspace bytes needed by fsg_simus_batched_tc. */
+size_t fsg_simus_batched_tc_workspace_size(const FsgProbe* probe, const FsgPhantom* phantoms, int32_t n_phantoms,
+                                           int32_t n_tx, const FsgBatchTuning* tuning);
+
+/*
+ * fsg_simus_batched on the tcgen05 tensor cores.  Same contract and outputs; the transmit
+ * contraction over elements and the receive contraction over scatterers run as complex GEMMs
+ * on BF16 hi + lo splits of Green's tiles generated on chip in FP32 (three products, FP32
+ * accumulation in TMEM).  Accuracy target relative L2 <= 1e-3 against the FP64 reference
+ * (measured ~1e-5).  Limits: n_elements <= 64, n_sub <= 2, n_tx <= 32.
+ * tuning->freqs_per_item (1..7, default 6) sets how many frequencies share one Green's
+ * geometry pass.  Every device-side wait is bounded; a wait that gives up records
+ * FSG_ETIMEOUT, readable with fsg_simus_batched_tc_status.
+ */
+int32_t fsg_simus_batched_tc(const FsgProbe* probe, const FsgMedium* medium, const FsgPhantom* phantoms,
+                             int32_t n_phantoms, const double* delays, const double* apod, int32_t n_tx,
+                             const FsgBatchTuning* tuning, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Synchronises `stream` and reads the device-side status word of the last fsg_simus_batched_tc
+ * call that used `workspace` (FSG_OK or FSG_ETIMEOUT) into *status_out. */
+int32_t fsg_simus_batched_tc_status(const void* workspace, const FsgProbe* probe, const FsgPhantom* phantoms,
+                                    int32_t n_phantoms, int32_t n_tx, const FsgBatchTuning* tuning,
+                                    int32_t* status_out, void* stream);
+
+/* Verification utility, no counterpart in the reference: one 128 x 64 x 64 tile of the
+ * tensor-core GEMM used by fsg_simus_batched_tc.  d[128][64] = a[128][64] * b[64][64]^T with
+ * a, b FP32 row-major on the device, split into BF16 hi/lo, placed K-major (0) or MN-major (1)
+ * in shared memory.  A bounded wait that gives up writes FSG_ETIMEOUT to *status (device int). */
+int32_t fsg_tc_selftest(const float* a, const float* b, float* d, int32_t a_mn_major, int32_t b_mn_major,
+                        int32_t* status, void* stream);
+
 /*
  * fsg_simus without a workspace argument, for callers that cannot allocate device memory
  * (for example a plugin whose host application owns all device memory and passes only input
