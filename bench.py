@@ -490,6 +490,149 @@ def run_batched_workload(args):
     print(json.dumps(line), flush=True)
 
 
+def _oracle_rf_shard(args):
+    import oracle.fastsimus_fp64 as O
+
+    scat, rc, delays, plan, params, medium = args
+    return O.simus_spectrum_selected(scat, rc, delays, plan, params, medium)
+
+
+def run_tc_workload(args):
+    """cfg4: 31 plane waves in [-12, 12] deg, 262,144 scatterers (5 % bright x10), cfg1 probe.
+    Times the tcgen05 BF16 hi/lo path, the FP32 batched path and the plain single-transmit
+    kernel looped over firings, and measures the tensor-core path's RF error against the FP64
+    oracle on 3 firings x a 16,384-scatterer subsample (linearity makes the subsample a valid
+    check of the same arithmetic)."""
+    import multiprocessing as mp
+
+    import torch
+
+    import fastsimus_gb300 as F
+    from fastsimus_gb300 import _device, build
+    from fastsimus_gb300 import workloads as W
+    from fastsimus_gb300.batched import BatchedSimus
+
+    _single_thread_blas()
+    build.build()
+    device = torch.device("cuda", _env_int("LOCAL_RANK", 0))
+    torch.cuda.set_device(device)
+    p, m = W.cfg1_probe(), W.cfg1_medium()
+    scat, rc = W.cfg4_scatterers(args.scatterers if args.scatterers != 200_000 else 262_144)
+    angles = np.linspace(-12.0, 12.0, 31)
+    delays = W.plane_wave_delays(p, m, angles)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
+
+    def time_graph(b, steps):
+        b.capture()
+        for _ in range(args.warmup):
+            b.replay()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(steps):
+            flush.zero_()
+            st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            st.record()
+            b.replay()
+            en.record()
+            torch.cuda.synchronize()
+            ms.append(st.elapsed_time(en))
+        return float(np.mean(ms))
+
+    if args.tc_only:  # profiling case: the tensor-core sweep alone
+        tc = BatchedSimus([(scat, rc)], delays, p, m, backend="tc")
+        for _ in range(max(1, args.steps)):
+            tc.launch_sweep()
+        torch.cuda.synchronize()
+        print(json.dumps({"tc_only": True, "status": tc.device_status()}), flush=True)
+        return
+    out = {}
+    with ClockSampler(device.index or 0) as clocks:
+        tc = BatchedSimus([(scat, rc)], delays, p, m, backend="tc")
+        plan = tc.plans[0]
+        best_tc = tc.autotune(cache=False)
+        tc_ms = time_graph(tc, args.steps)
+        assert tc.device_status() == 0
+        tc_spec = tc.outs[0].clone()
+        fp = BatchedSimus([(scat, rc)], delays, p, m, plans=[plan], backend="fp32")
+        fp_ms = time_graph(fp, max(1, args.steps // 2))
+        fp_spec = fp.outs[0].clone()
+        # plain single-transmit kernel, one call per firing (the reference's usage)
+        scat_d, rc_d = torch.as_tensor(scat, device=device), torch.as_tensor(rc, device=device)
+        del_d = torch.as_tensor(delays, device=device)
+        for t in range(2):
+            F.simus_compute(scat_d, rc_d, del_d[t], plan, p, m)
+        torch.cuda.synchronize()
+        flush.zero_()
+        st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        st.record()
+        plain_spec = [F.simus_compute(scat_d, rc_d, del_d[t], plan, p, m).spectrum for t in range(len(angles))]
+        en.record()
+        torch.cuda.synchronize()
+        plain_ms = st.elapsed_time(en)
+    plain = torch.stack(plain_spec, 0)
+
+    def rel(a, b):
+        a, b = a.to(torch.complex128), b.to(torch.complex128)
+        return float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
+
+    # accuracy of the tensor-core path against the FP64 oracle on a subsample
+    n_sub_s = args.tc_oracle_scatterers
+    sub = np.random.default_rng(5).choice(scat.shape[0], n_sub_s, replace=False)
+    firings = [0, len(angles) // 2, len(angles) - 1]
+    tc_sub = BatchedSimus([(scat[sub], rc[sub])], delays, p, m, plans=[plan], backend="tc")
+    tc_sub.run()
+    sub_spec = tc_sub.outs[0].cpu().numpy()
+    model, cores = _cpu_info()
+    errs, phases = [], []
+    i0, nf = plan.freq_idx_start, plan.selected_freqs.shape[0]
+    with mp.get_context("spawn").Pool(cores) as pool:
+        for t in firings:
+            shards = np.array_split(sub, cores)
+            parts = pool.map(_oracle_rf_shard, [(scat[i], rc[i], delays[t], plan, p, m) for i in shards])
+            ref_sel = sum(parts) * plan.correction_factor
+            got = sub_spec[t, i0:i0 + nf].astype(np.complex128)
+            errs.append(float(np.linalg.norm(got - ref_sel) / np.linalg.norm(ref_sel)))
+            mask = np.abs(ref_sel) > 1e-3 * np.abs(ref_sel).max()
+            phases.append(float(np.max(np.abs(np.angle(got[mask] / ref_sel[mask])))))
+    frames = len(angles)
+    E, U, Fq = p.n_elements, plan.n_sub, plan.selected_freqs.shape[0]
+    terms = scat.shape[0] * E * U * Fq * frames
+    alg = algorithmic_flops_simus(plan, p, scat.shape[0], n_tx=frames)
+    tensor_flops = 3 * 2 * (2 * 128 * 64 * 64) * (scat.shape[0] / 64) * Fq  # executed: TX + RX real GEMMs x 3 products
+    peaks = _peaks()
+    bf16_peak = peaks.get("bf16_tflops", 1890.4)
+    line = {
+        "metric": "RF frames/s & Green terms/s: tcgen05 BF16 hi/lo path vs plain FP32 kernel at relL2<=1e-3",
+        "value": frames / (tc_ms * 1e-3), "unit": "frames/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": tc_ms, "higher_is_better": True, "dtype": "bf16x3 (hi/lo) tensor, f32 accumulate",
+        "data": "synthetic (seeded)",
+        "config": {"workload": f"cfg4: cfg1 probe, 31 plane waves in [-12,12] deg, {scat.shape[0]} scatterers, "
+                               "5% x10 bright", "n_freq": int(Fq), "tuning_tc": best_tc.__dict__,
+                   "l2": "flushed before every timed step"},
+        "green_terms_per_s": terms / (tc_ms * 1e-3),
+        "paths": {
+            "tc": {"frames_per_s": frames / (tc_ms * 1e-3), "green_terms_per_s": terms / (tc_ms * 1e-3),
+                   "ms_per_batch": tc_ms, "relL2_vs_plain_fp32": rel(tc_spec, plain),
+                   "relL2_vs_fp64_oracle": errs, "max_phase_err_rad_vs_fp64": phases,
+                   "oracle_subset": f"firings {firings} (angles {[float(angles[i]) for i in firings]}) on "
+                                    f"{n_sub_s} random scatterers, oracle on {cores} cores"},
+            "fp32_batched": {"frames_per_s": frames / (fp_ms * 1e-3), "green_terms_per_s": terms / (fp_ms * 1e-3),
+                             "ms_per_batch": fp_ms, "relL2_vs_plain_fp32": rel(fp_spec, plain)},
+            "plain_fp32_single_transmit": {"frames_per_s": frames / (plain_ms * 1e-3),
+                                           "green_terms_per_s": terms / (plain_ms * 1e-3),
+                                           "ms_per_batch": plain_ms},
+        },
+        "speedup_tc_vs_plain": plain_ms / tc_ms, "speedup_tc_vs_fp32_batched": fp_ms / tc_ms,
+        "roofline": {"kernel": "tc_kernel", "bound": "tensor", "achieved": tensor_flops / (tc_ms * 1e-3) / 1e12,
+                     "peak": bf16_peak, "unit": "TFLOP/s", "frac": tensor_flops / (tc_ms * 1e-3) / 1e12 / bf16_peak,
+                     "peak_source": "MEASURED_PEAKS.json bf16_tflops (measured)" if "bf16_tflops" in peaks
+                     else "fallback 1890.4", "note": "executed bf16 tensor flops (3 hi/lo products); "
+                     "algorithmic (complex, once) TFLOP/s: " + f"{alg / (tc_ms * 1e-3) / 1e12:.1f}"},
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -503,8 +646,11 @@ def main():
     ap.add_argument("--scatterers", type=int, default=200_000, help="smaller values make profiling cases")
     ap.add_argument("--grid-nx", type=int, default=256)
     ap.add_argument("--grid-nz", type=int, default=512)
-    ap.add_argument("--workload", choices=["cfg2", "cfg3"], default="cfg2",
-                    help="cfg2: plain simus + pfield frame (default); cfg3: batched 75 waves x 16 phantoms")
+    ap.add_argument("--workload", choices=["cfg2", "cfg3", "cfg4"], default="cfg2",
+                    help="cfg2: plain simus + pfield frame (default); cfg3: batched 75 waves x 16 phantoms; "
+                         "cfg4: tensor-core path vs FP32 paths, 31 waves x 262,144 scatterers")
+    ap.add_argument("--tc-oracle-scatterers", type=int, default=16384)
+    ap.add_argument("--tc-only", action="store_true", help="cfg4 profiling case: only the tensor-core sweep")
     ap.add_argument("--phantoms", type=int, default=16)
     ap.add_argument("--transmits", type=int, default=75)
     args = ap.parse_args()
@@ -513,6 +659,8 @@ def main():
         run_reference_arm(args, rank, world)
     elif args.workload == "cfg3":
         run_batched_workload(args)
+    elif args.workload == "cfg4":
+        run_tc_workload(args)
     else:
         run_gpu_arm(args, rank, world)
 

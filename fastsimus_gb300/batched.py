@@ -42,7 +42,7 @@ class BatchTuning:
 
     @staticmethod
     def default(backend: str) -> "BatchTuning":
-        return BatchTuning(6, 65536, 1) if backend == "tc" else BatchTuning()
+        return BatchTuning(7, 65536, 1) if backend == "tc" else BatchTuning()
 
     def to_c(self) -> _native.FsgBatchTuning:
         return _native.FsgBatchTuning(self.freqs_per_item, self.chunk_scatterers, self.ctas_per_sm, 0)

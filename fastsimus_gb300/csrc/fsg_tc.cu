@@ -53,13 +53,44 @@ struct TcArgs {
   float2* partial;  // [n_items][fb][kTcTx][kTcE]
 };
 
-// Geometry for the tensor-core path: same distance / amplitude / anchor as the plain kernels;
-// the recurrence step comes from the MUFU sin/cos (its ~4e-7 error compounds over < 7 steps).
+// Geometry for the tensor-core path (accuracy target 1e-3): double-float distance and anchor
+// phase as in the plain kernels, but the square root comes from one rsqrt plus a correction,
+// and the recurrence step uses the MUFU sin/cos/exp2 -- its ~4e-7 error compounds over at most
+// six steps.
 __device__ __forceinline__ void tc_source(dfl xs, dfl zs, float4 sp, float2 rot, const SweepConst& C, float2 k0,
                                           float a0, float2& g, float2& st) {
-  const SrcGeo geo = source_geometry(xs, zs, sp, rot, C);
-  g = anchor_value(geo.r_hi, geo.r_lo, geo.amp, k0, a0);
-  st = geo.step;
+  const dfl dx = df_add(xs, dfl{-sp.x, -sp.y});
+  const dfl dz = df_add(zs, dfl{-sp.z, -sp.w});
+  const dfl d2 = df_add(df_sqr(dx), df_sqr(dz));
+  float r_hi, r_lo, rinv;
+  if (d2.hi > 0.0f) {
+    rinv = rsqrtf(d2.hi);
+    const float r0 = d2.hi * rinv;
+    const float res = __fadd_rn(fmaf(-r0, r0, d2.hi), d2.lo);  // d2 - r0^2
+    const dfl r = fast_two_sum(r0, res * (0.5f * rinv));
+    r_hi = r.hi;
+    r_lo = r.lo;
+  } else {
+    r_hi = r_lo = 0.0f;
+    rinv = 0.0f;
+  }
+  float a = (r_hi > 0.0f) ? dx.hi * rinv : 1.0f;
+  a = fminf(1.0f, fmaxf(-1.0f, a));
+  const float ca = sqrtf((1.0f - a) * (1.0f + a));
+  const float sth = fmaf(a, rot.x, -ca * rot.y);
+  const float cth = fmaf(ca, rot.x, a * rot.y);
+  if (r_hi < C.min_dist.x || (r_hi == C.min_dist.x && r_lo < C.min_dist.y)) {
+    r_hi = C.min_dist.x;
+    r_lo = C.min_dist.y;
+  }
+  float ob = (C.baffle == 0) ? cth : ((C.baffle == 1) ? 1.0f : __fdividef(cth, cth + C.baffle_val));
+  if (cth <= 0.0f) ob = 1e-16f;
+  const float amp = ob * sinc_rad(C.dir_coef * sth) * rsqrtf(r_hi) * C.inv_nsub;
+  g = anchor_value(r_hi, r_lo, amp, k0, a0);
+  float sn, cs;
+  __sincosf(C.dk.x * r_hi, &sn, &cs);
+  const float mag = __expf(-C.dalpha * r_hi);
+  st = make_float2(mag * cs, mag * sn);
 }
 
 // SMEM layout (bytes).
@@ -69,8 +100,10 @@ constexpr uint32_t kOffArxHi = 32768;             // MN-major 128 x 64 bf16
 constexpr uint32_t kOffArxLo = 49152;
 constexpr uint32_t kOffBrxHi = 65536;             // MN-major 64 (n) x 64 (k)
 constexpr uint32_t kOffBrxLo = 73728;
-constexpr uint32_t kOffX = 81920;                 // exchange: 2 x 64 x 32 floats
-constexpr uint32_t kOffBtx = 98304;               // per band frequency: K-major 64 x 64, hi then lo
+constexpr uint32_t kOffX = 81920;                 // exchange: 2 x 64 rows x 33 floats (padded: conflict-free)
+constexpr int kXPitch = 33;
+constexpr uint32_t kOffBtx = 99328;               // per band frequency: K-major 64 x 64, hi then lo
+static_assert(kOffX + 2 * 64 * kXPitch * 4 <= kOffBtx, "exchange buffer overlaps the transmit operands");
 constexpr uint32_t kBtxBytes = 16384;
 
 __host__ __device__ constexpr uint32_t tc_smem_bytes(int fb) { return kOffBtx + (uint32_t)fb * kBtxBytes + 1024; }
@@ -199,11 +232,11 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
             const int e = eg * 16 + idx / U, u = idx % U;
             float2 g = make_float2(0.f, 0.f), st = make_float2(0.f, 0.f);
             if (sval && e < E) tc_source(xs, zs, A.src_pos[e * U + u], A.rot_e[e], C, k0, a0, g, st);
-            stage[tid * 8 + i] = make_float4(g.x, g.y, st.x, st.y);
+            stage[i * kThreads + tid] = make_float4(g.x, g.y, st.x, st.y);
           }
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
-            const float4 v = stage[tid * 8 + i];
+            const float4 v = stage[i * kThreads + tid];
             G[c * 8 + i] = make_float2(v.x, v.y);
             S[c * 8 + i] = make_float2(v.z, v.w);
           }
@@ -288,12 +321,12 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
         const int row = 32 * q + lane;  // (c, s) with c = row / 64
         if (row >= 64) {
 #pragma unroll
-          for (int t = 0; t < 32; ++t) X[(h * 64 + (row - 64)) * 32 + t] = v[t];
+          for (int t = 0; t < 32; ++t) X[(h * 64 + (row - 64)) * kXPitch + t] = v[t];
         }
         __syncthreads();
         if (row < 64) {
           // h = 0: Pr = D[0,s][0,t] - D[1,s][1,t];  h = 1: Pi = D[0,s][1,t] + D[1,s][0,t]
-          const float* x = X + ((1 - h) * 64 + row) * 32;
+          const float* x = X + ((1 - h) * 64 + row) * kXPitch;
 #pragma unroll
           for (int t = 0; t < 32; ++t) v[t] = h ? v[t] + x[t] : v[t] - x[t];
 #pragma unroll
@@ -347,11 +380,11 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
       const int row = 32 * q + lane;  // (c, e)
       if (row >= 64) {
 #pragma unroll
-        for (int t = 0; t < 32; ++t) X[(h * 64 + (row - 64)) * 32 + t] = have ? v[t] : 0.f;
+        for (int t = 0; t < 32; ++t) X[(h * 64 + (row - 64)) * kXPitch + t] = have ? v[t] : 0.f;
       }
       __syncthreads();
       if (row < 64) {
-        const float* x = X + ((1 - h) * 64 + row) * 32;
+        const float* x = X + ((1 - h) * 64 + row) * kXPitch;
 #pragma unroll
         for (int t = 0; t < 32; ++t) {
           const float val = have ? (h ? v[t] + x[t] : v[t] - x[t]) : 0.f;
@@ -477,7 +510,7 @@ struct TcLayout {
 
 void tc_layout(const FsgProbe* probe, const FsgPhantom* ph, int n_ph, int n_tx, const FsgBatchTuning* tu,
                TcLayout* L) {
-  int fb = (tu && tu->freqs_per_item > 0) ? tu->freqs_per_item : 6;
+  int fb = (tu && tu->freqs_per_item > 0) ? tu->freqs_per_item : 7;
   if (fb > kTcMaxFb) fb = kTcMaxFb;
   L->fb = fb;
   int64_t chunk = (tu && tu->chunk_scatterers > 0) ? tu->chunk_scatterers : 65536;
