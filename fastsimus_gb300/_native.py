@@ -83,6 +83,18 @@ _SIGNATURES = {
     "fsg_simus_batched_tc_status": (ctypes.c_int32, [_P, ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgPhantom),
                                                      ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(FsgBatchTuning),
                                                      ctypes.POINTER(ctypes.c_int32), _P]),
+    "fsg_simus_batched_rx": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgMedium),
+                                              ctypes.POINTER(FsgPhantom), _P, ctypes.c_int32, _P,
+                                              ctypes.POINTER(FsgBatchTuning), _P, ctypes.c_size_t, _P]),
+    "fsg_txfield": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgMedium), ctypes.c_double,
+                                     ctypes.c_double, _P, ctypes.c_int64, _P, _P, ctypes.c_size_t, _P]),
+    "fsg_mlp_gemm": (ctypes.c_int32, [_P, ctypes.c_int64, ctypes.c_int64, _P, ctypes.c_int64, ctypes.c_int64,
+                                      ctypes.c_int32, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+                                      ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P]),
+    "fsg_mlp_features": (ctypes.c_int32, [_P, _P, _P, ctypes.c_int64, _P]),
+    "fsg_mlp_colsum": (ctypes.c_int32, [_P, ctypes.c_int64, ctypes.c_int32, _P, ctypes.c_int32, _P]),
+    "fsg_mlp_adam": (ctypes.c_int32, [_P, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_float, ctypes.c_float,
+                                      ctypes.c_float, ctypes.c_float, ctypes.c_int32, ctypes.c_float, _P]),
     "fsg_tc_selftest": (ctypes.c_int32, [_P, _P, _P, ctypes.c_int32, ctypes.c_int32, _P, _P]),
     "fsg_simus_noalloc": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgMedium),
                                            ctypes.POINTER(FsgFreqPlan), _P, _P, ctypes.c_int64, _P, _P, ctypes.c_int32,

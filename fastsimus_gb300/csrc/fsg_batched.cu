@@ -158,33 +158,47 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
 #pragma unroll
       for (int f = 0; f < FB; ++f) {
         const float2* G = Gm + f * kBT * kGmPitch;
-        // --- TX: P[s][t] = sum_e G[s][e] D[e][t]; thread rows s = wm*16 + lm + 4i, cols t = wn*40 + ln*5 + j
-        float2 acc[4][5];
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-          for (int j = 0; j < 5; ++j) acc[i][j] = make_float2(0.f, 0.f);
-        const float2* Df = D + f * kBE * kWPitch;
-#pragma unroll 4
-        for (int e = 0; e < kBE; ++e) {
-          float2 a[4], b[5];
-#pragma unroll
-          for (int i = 0; i < 4; ++i) a[i] = G[(wm * 16 + lm + 4 * i) * kGmPitch + e];
-#pragma unroll
-          for (int j = 0; j < 5; ++j) b[j] = Df[e * kWPitch + wn * 40 + ln * 5 + j];
-#pragma unroll
+        if (A.tx_in) {
+          // transmit field supplied by the caller (already includes pulse * probe): W = rc * p
+          for (int i = tid; i < kBT * kBTX; i += kThreads) {
+            const int sl = i / kBTX, t = i % kBTX;
+            const int64_t sg = t0 + sl;
+            float2 v = make_float2(0.f, 0.f);
+            if (sg < s_end && t < T && f < nf) {
+              const float2 pv = A.tx_in[((size_t)sg * P.n_freq + (f0 + f)) * T + t];
+              v = make_float2(rcs[sl] * pv.x, rcs[sl] * pv.y);
+            }
+            W[sl * kWPitch + t] = v;
+          }
+        } else {
+          // --- TX: P[s][t] = sum_e G[s][e] D[e][t]; thread rows s = wm*16 + lm + 4i, cols t = wn*40 + ln*5 + j
+          float2 acc[4][5];
+  #pragma unroll
           for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int j = 0; j < 5; ++j) acc[i][j] = cfma(a[i], b[j], acc[i][j]);
-        }
-        // W[s][t] = rc_s * pulse * probe * P
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const int s = wm * 16 + lm + 4 * i;
-          const float w = rcs[s];
-          const float2 sc = make_float2(w * pp[f].x, w * pp[f].y);
-#pragma unroll
-          for (int j = 0; j < 5; ++j) W[s * kWPitch + wn * 40 + ln * 5 + j] = cmul(sc, acc[i][j]);
+  #pragma unroll
+            for (int j = 0; j < 5; ++j) acc[i][j] = make_float2(0.f, 0.f);
+          const float2* Df = D + f * kBE * kWPitch;
+  #pragma unroll 4
+          for (int e = 0; e < kBE; ++e) {
+            float2 a[4], b[5];
+  #pragma unroll
+            for (int i = 0; i < 4; ++i) a[i] = G[(wm * 16 + lm + 4 * i) * kGmPitch + e];
+  #pragma unroll
+            for (int j = 0; j < 5; ++j) b[j] = Df[e * kWPitch + wn * 40 + ln * 5 + j];
+  #pragma unroll
+            for (int i = 0; i < 4; ++i)
+  #pragma unroll
+              for (int j = 0; j < 5; ++j) acc[i][j] = cfma(a[i], b[j], acc[i][j]);
+          }
+          // W[s][t] = rc_s * pulse * probe * P
+  #pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const int s = wm * 16 + lm + 4 * i;
+            const float w = rcs[s];
+            const float2 sc = make_float2(w * pp[f].x, w * pp[f].y);
+  #pragma unroll
+            for (int j = 0; j < 5; ++j) W[s * kWPitch + wn * 40 + ln * 5 + j] = cmul(sc, acc[i][j]);
+          }
         }
         __syncthreads();
         // --- RX: Y[e][t] += sum_s G[s][e] W[s][t]; thread rows e = wm*16 + lm + 4i
@@ -371,10 +385,10 @@ extern "C" size_t fsg_simus_batched_workspace_size(const FsgProbe* probe, const 
   return L.total;
 }
 
-extern "C" int32_t fsg_simus_batched(const FsgProbe* probe, const FsgMedium* medium, const FsgPhantom* phantoms,
-                                     int32_t n_phantoms, const double* delays, const double* apod, int32_t n_tx,
-                                     const FsgBatchTuning* tuning, void* workspace, size_t workspace_bytes,
-                                     void* stream_ptr) {
+static int32_t simus_batched_impl(const FsgProbe* probe, const FsgMedium* medium, const FsgPhantom* phantoms,
+                                  int32_t n_phantoms, const double* delays, const double* apod, int32_t n_tx,
+                                  const FsgBatchTuning* tuning, const float2* tx_in, void* workspace,
+                                  size_t workspace_bytes, void* stream_ptr) {
   int st = validate_batch(probe, medium, phantoms, n_phantoms, delays, n_tx);
   if (st != FSG_OK) return st;
   BatchPlanLayout L;
@@ -486,6 +500,7 @@ extern "C" int32_t fsg_simus_batched(const FsgProbe* probe, const FsgMedium* med
     convex_geometry(probe, &A.convex, &A.apex, &A.radius2);
     A.queue = queue;
     A.partial = partial;
+    A.tx_in = tx_in;
     const int per_sm = (tuning && tuning->ctas_per_sm > 0) ? tuning->ctas_per_sm : 1;
     int grid = sms * per_sm;
     if (grid > L.n_items) grid = L.n_items;
@@ -505,4 +520,21 @@ extern "C" int32_t fsg_simus_batched(const FsgProbe* probe, const FsgMedium* med
     if ((st = check_cuda(cudaGetLastError(), "batched_reduce launch")) != FSG_OK) return st;
   }
   return FSG_OK;
+}
+
+extern "C" int32_t fsg_simus_batched(const FsgProbe* probe, const FsgMedium* medium, const FsgPhantom* phantoms,
+                                     int32_t n_phantoms, const double* delays, const double* apod, int32_t n_tx,
+                                     const FsgBatchTuning* tuning, void* workspace, size_t workspace_bytes,
+                                     void* stream) {
+  return simus_batched_impl(probe, medium, phantoms, n_phantoms, delays, apod, n_tx, tuning, nullptr, workspace,
+                            workspace_bytes, stream);
+}
+
+extern "C" int32_t fsg_simus_batched_rx(const FsgProbe* probe, const FsgMedium* medium, const FsgPhantom* phantom,
+                                        const double* delays, int32_t n_tx, const void* tx_field,
+                                        const FsgBatchTuning* tuning, void* workspace, size_t workspace_bytes,
+                                        void* stream) {
+  if (!tx_field) return fsg::set_error(FSG_EINVAL, "tx_field must be non-NULL");
+  return simus_batched_impl(probe, medium, phantom, 1, delays, nullptr, n_tx, tuning,
+                            static_cast<const float2*>(tx_field), workspace, workspace_bytes, stream);
 }

@@ -43,6 +43,7 @@ struct BatchArgs {
   double apex, radius2;
   int* queue;
   float2* partial;          // [n_items][fb][80][64]
+  const float2* tx_in;      // optional [n_scat][n_freq][n_tx] transmit field (phantom 0); NULL = compute
 };
 
 struct BatchSetupArgs {

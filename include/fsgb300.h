@@ -200,6 +200,45 @@ int32_t fsg_tc_selftest(const float* a, const float* b, float* d, int32_t a_mn_m
                         int32_t* status, void* stream);
 
 /*
+ * fsg_simus_batched for one phantom whose transmit field is supplied by the caller instead of
+ * computed: tx_field is device complex64 [n_scat][plan.n_freq][n_tx], the pressure
+ * pulse*probe*sum_src(...) of each firing at each scatterer and selected frequency (e.g. from a
+ * surrogate network).  Only the receive contraction over scatterers runs.  No counterpart in
+ * the reference: it is how a learned transmit field drops into the simus sweep
+ * (_simus_strategies.py:64-73 with p_k given).
+ */
+int32_t fsg_simus_batched_rx(const FsgProbe* probe, const FsgMedium* medium, const FsgPhantom* phantom,
+                             const double* delays, int32_t n_tx, const void* tx_field, const FsgBatchTuning* tuning,
+                             void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * Exact complex transmit pressure of a plane wave at arbitrary samples (x, z, f, theta)
+ * (device float64 [n][4]; metres, Hz, radians; linear arrays, unit apodization), for
+ * training and judging a surrogate.  Closed form of the pressure inside
+ * _pfield_strategies.py:48 (before |.|^2) with the plane-wave delays of tx_delay.py:116-189.
+ * out: device complex64 [n].  workspace >= n_elements*n_sub*16 + n_elements*8 + 1024 bytes.
+ */
+int32_t fsg_txfield(const FsgProbe* probe, const FsgMedium* medium, double tx_n_wavelengths, double bandwidth,
+                    const double* samples, int64_t n, void* out, void* workspace, size_t workspace_bytes,
+                    void* stream);
+
+/* MLP building blocks of the transmit-field surrogate (no counterpart in the reference).
+ * fsg_mlp_gemm: C[m][n] = sum_k A(m,k) B(k,n) with A(m,k) = A[m*a_sm + k*a_sk] (float32),
+ * B(k,n) = B[k*b_sk + n*b_sn] (bfloat16 if b_bf16 else float32), FP32 accumulation, and a
+ * fused epilogue: 0 = (+bias[n]) (accumulate into C if `accumulate`), 1 = C = acc + bias[n],
+ * C2 = silu(C), 2 = C = acc * silu'(Zs[m][n]).  C, C2, Zs have row stride ldc. */
+int32_t fsg_mlp_gemm(const float* A, int64_t a_sm, int64_t a_sk, const void* B, int64_t b_sk, int64_t b_sn,
+                     int32_t b_bf16, const float* bias, const float* Zs, float* C, float* C2, int64_t ldc, int32_t M,
+                     int32_t N, int32_t K, int32_t epilogue, int32_t accumulate, void* stream);
+/* feat[n][j] = sin(2 pi B_j . u_n), feat[n][64+j] = cos(2 pi B_j . u_n), B: [64][4], u: [n][4]. */
+int32_t fsg_mlp_features(const float* u, const float* bmat, float* feat, int64_t n, void* stream);
+/* out[n] (+)= sum_m X[m][n], X: [M][N] float32. */
+int32_t fsg_mlp_colsum(const float* X, int64_t M, int32_t N, float* out, int32_t accumulate, void* stream);
+/* One Adam step on float32 master weights w (and their bfloat16 copy w_bf16, if non-NULL). */
+int32_t fsg_mlp_adam(float* w, void* w_bf16, const float* grad, float* m1, float* m2, int64_t n, float lr, float b1,
+                     float b2, float eps, int32_t step, float grad_scale, void* stream);
+
+/*
  * fsg_simus without a workspace argument, for callers that cannot allocate device memory
  * (for example a plugin whose host application owns all device memory and passes only input
  * and output buffers).  No counterpart in the reference: it is fsg_simus running on a 16 MiB

@@ -563,3 +563,39 @@ def diverging_wave(element_pos, tilt_rad, width_rad, *, aperture_length, speed_o
     z0 = sc * aperture_length / den
     x0 = sc * z0 * tan(width_rad / 2 - tn) + aperture_length / 2
     return focused(element_pos, np.asarray([x0, z0]), speed_of_sound=speed_of_sound)
+
+
+# --------------------------------------------------------------------------------------
+# transmit field at (x, z, f, theta) samples, for the surrogate (closed form, FP64)
+# --------------------------------------------------------------------------------------
+
+
+def tx_field_samples(samples, params, medium, tx_n_wavelengths=1.0, n_sub=None):
+    """Complex transmit pressure of a plane wave at samples (n, 4) = (x, z, f, theta):
+    pulse(f) probe(f) * sum_{e,u} exp(i 2 pi f tau_e) G(x, z, e, u, f) / n_sub, where G is the
+    closed form of _init_exponentials (_pfield_math.py:202-247) at frequency f with the
+    centre-frequency directivity (pfield.py:148-152) and tau_e the plane-wave delays
+    (tx_delay.py:116-189).  Equals the pressure inside _pfield_strategies.py:48 for
+    f on a plan's grid."""
+    samples = np.asarray(samples, dtype=np.float64).reshape(-1, 4)
+    c = medium.speed_of_sound
+    if n_sub is None:
+        n_sub = _auto_n_sub(params, c, None)
+    epos, theta_e, _ = element_positions(params.n_elements, params.pitch, params.radius)
+    theta_e = np.zeros(params.n_elements) if theta_e is None else theta_e
+    offs = subelement_centroids(params.element_width, n_sub, theta_e)
+    seg = params.element_width / n_sub
+    out = np.zeros(samples.shape[0], dtype=np.complex128)
+    kc = 2.0 * pi * params.freq_center / c
+    for i, (x, z, f, th) in enumerate(samples):
+        dist, sin_t, theta = distances_and_angles(np.array([x, z]), offs, epos, theta_e, c, params.freq_center)
+        ob = obliquity_factor(theta, params.baffle)
+        init, _ = init_exponentials(f, c, medium.attenuation, dist, ob, 0.0)
+        init = init * np.sinc(kc * seg / 2.0 * sin_t / pi)
+        tau = plane_wave(epos, th, speed_of_sound=c)
+        w = 2.0 * pi * f
+        spec = pulse_spectrum(np.array([w]), params.freq_center, tx_n_wavelengths)[0] * \
+            probe_spectrum(np.array([w]), params.freq_center, params.bandwidth)[0]
+        p = spec * np.sum(init * np.exp(1j * 2.0 * pi * f * tau)[:, None]) / n_sub
+        out[i] = 0.0 if z < 0 else p
+    return out
