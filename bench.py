@@ -417,9 +417,38 @@ def run_gpu_arm(args, rank, world):
             "value": 1.0 / t, "unit": UNIT, "cores": cores, "kind": "port", "cpu": model,
             "sample": f"{args.cpu_scatterers} scatterers + {args.cpu_points} grid points of the frame, sharded over "
                       f"{cores} processes, scaled linearly to 200,000 scatterers + 131,072 points"}
+    if not args.no_paths and world == 1:
+        line["paths"] = other_paths(args)
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def other_paths(args) -> dict:
+    """Summaries of the batched (cfg3), tensor-core (cfg4) and surrogate (cfg5) paths, measured
+    in the same run; a failure in one is recorded in the line, not raised."""
+    import copy
+
+    out = {}
+    for name, fn, kw in (("batched_fp32_cfg3", run_batched_workload, {"autotune_quick": True}),
+                         ("tensor_core_cfg4", run_tc_workload, {}),
+                         ("surrogate_cfg5", run_surrogate_workload, {})):
+        a = copy.copy(args)
+        a.scatterers = 200_000  # each workload uses its own size
+        a.steps, a.warmup = 3, 2
+        for k, v in kw.items():
+            setattr(a, k, v)
+        try:
+            r = fn(a)
+            keep = ("metric", "value", "unit", "ms_per_step", "green_terms_per_s", "sweep_ms", "roofline", "paths",
+                    "speedup_tc_vs_plain", "speedup_tc_vs_fp32_batched", "config", "training",
+                    "field_rel_l2_1M_queries", "per_query_s", "simus_1M_x75", "clocks")
+            out[name] = {k: r[k] for k in keep if k in r}
+            if "training" in out[name]:
+                out[name]["training"] = {k: v for k, v in out[name]["training"].items() if k != "history"}
+        except Exception as exc:  # recorded in the JSON line
+            out[name] = {"error": f"{type(exc).__name__}: {exc}"}
+    return out
 
 
 def run_batched_workload(args):
@@ -435,13 +464,16 @@ def run_batched_workload(args):
     device = torch.device("cuda", _env_int("LOCAL_RANK", 0))
     torch.cuda.set_device(device)
     p, m = W.cfg1_probe(), W.cfg1_medium()
-    phantoms = W.cfg3_phantoms(args.phantoms)
-    delays = W.plane_wave_delays(p, m, np.linspace(-16.0, 16.0, args.transmits))
+    phantoms = W.cfg3_phantoms(getattr(args, "phantoms", 16))
+    delays = W.plane_wave_delays(p, m, np.linspace(-16.0, 16.0, getattr(args, "transmits", 75)))
     t0 = time.perf_counter()
     b = BatchedSimus(phantoms, delays, p, m)
     t_plan = time.perf_counter() - t0
     t0 = time.perf_counter()
-    best = b.autotune(cache=False)
+    from fastsimus_gb300.batched import BatchTuning
+
+    quick = [BatchTuning(1, 65536, 1), BatchTuning(2, 65536, 1)] if getattr(args, "autotune_quick", False) else None
+    best = b.autotune(candidates=quick, cache=False)
     t_tune = time.perf_counter() - t0
     b.capture()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
@@ -487,7 +519,7 @@ def run_batched_workload(args):
                          "peak": peak, "unit": "TFLOP/s", "frac": flops / (sweep_ms * 1e-3) / 1e12 / peak,
                          "algorithmic_flops_per_launch": flops},
             "autotune_log": getattr(b, "tune_log", None), "clocks": clocks.summary()}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def _oracle_rf_shard(args):
@@ -517,7 +549,7 @@ def run_tc_workload(args):
     device = torch.device("cuda", _env_int("LOCAL_RANK", 0))
     torch.cuda.set_device(device)
     p, m = W.cfg1_probe(), W.cfg1_medium()
-    scat, rc = W.cfg4_scatterers(args.scatterers if args.scatterers != 200_000 else 262_144)
+    scat, rc = W.cfg4_scatterers(args.scatterers if args.scatterers != 200_000 else 262_144)  # 262,144 by default
     angles = np.linspace(-12.0, 12.0, 31)
     delays = W.plane_wave_delays(p, m, angles)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
@@ -543,8 +575,7 @@ def run_tc_workload(args):
         for _ in range(max(1, args.steps)):
             tc.launch_sweep()
         torch.cuda.synchronize()
-        print(json.dumps({"tc_only": True, "status": tc.device_status()}), flush=True)
-        return
+        return {"tc_only": True, "status": tc.device_status()}
     out = {}
     with ClockSampler(device.index or 0) as clocks:
         tc = BatchedSimus([(scat, rc)], delays, p, m, backend="tc")
@@ -630,7 +661,91 @@ def run_tc_workload(args):
                      "algorithmic (complex, once) TFLOP/s: " + f"{alg / (tc_ms * 1e-3) / 1e12:.1f}"},
         "clocks": clocks.summary(),
     }
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def run_surrogate_workload(args):
+    """cfg5: Fourier-feature MLP (64 features, 4 x 256 SiLU, BF16 weights) trained on the GPU by
+    the library's own kernels on 2M exact transmit-field samples over the cfg1 box, the band
+    fc (1 +- B/2) and +-16 deg; then used in simus for 1,000,000 scatterers x 75 plane waves with
+    the exact kernel judging every 64-scatterer tile and recomputing tiles above 1e-3.  The
+    simus part runs on a bounded sample of the phantom and is scaled by scatterer count;
+    the exact FP32 batched sweep is timed on the full phantom."""
+    import torch
+
+    from fastsimus_gb300 import build
+    from fastsimus_gb300 import workloads as W
+    from fastsimus_gb300.batched import BatchedSimus, shared_plan
+    from fastsimus_gb300.surrogate import TxFieldSurrogate, cfg5_box, simus_with_surrogate
+
+    build.build()
+    device = torch.device("cuda", _env_int("LOCAL_RANK", 0))
+    torch.cuda.set_device(device)
+    p, m = W.cfg1_probe(), W.cfg1_medium()
+    sur = TxFieldSurrogate(p, m, cfg5_box(p), seed=0)
+    rep = sur.train(n_train=args.sur_train, epochs=args.sur_epochs, batch=4096)
+    # per-query costs: network inference vs exact field
+    q = sur.sample_domain(1 << 20, seed=9)
+    for _ in range(2):
+        sur.predict(q)
+        sur.exact(q)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ev[0].record()
+    pred = sur.predict(q)
+    ev[1].record()
+    ex = sur.exact(q)
+    ev[2].record()
+    torch.cuda.synchronize()
+    t_net_q = ev[0].elapsed_time(ev[1]) * 1e-3 / q.shape[0]
+    t_exact_q = ev[1].elapsed_time(ev[2]) * 1e-3 / q.shape[0]
+    val_rel = float(torch.linalg.vector_norm(pred - ex) / torch.linalg.vector_norm(ex))
+    # the 1M x 75 use case
+    full_s, full_rc = W.cfg4_scatterers(1_000_000, seed=1)
+    angles = np.deg2rad(np.linspace(-16.0, 16.0, 75))
+    delays = W.plane_wave_delays(p, m, np.rad2deg(angles))
+    plan = shared_plan(full_s, full_rc, list(delays), p, m)
+    sub = np.random.default_rng(2).choice(full_s.shape[0], args.sur_sample, replace=False)
+    simus_with_surrogate(sur, full_s[sub[:128]], full_rc[sub[:128]], angles, plan, tol=1e-3)  # warm-up
+    res = simus_with_surrogate(sur, full_s[sub], full_rc[sub], angles, plan, tol=1e-3)
+    loose = simus_with_surrogate(sur, full_s[sub], full_rc[sub], angles, plan, tol=float("inf"))
+    ex_full = BatchedSimus([(full_s, full_rc)], delays, p, m, plans=[plan], backend="fp32")
+    ex_full.run()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ex_full.run()
+    torch.cuda.synchronize()
+    t_exact_full = time.perf_counter() - t0
+    scale = full_s.shape[0] / args.sur_sample
+    t_sur_full = res["t_surrogate_total_s"] * scale
+    frames = len(angles)
+    terms = full_s.shape[0] * p.n_elements * plan.n_sub * plan.selected_freqs.shape[0] * frames
+    line = {
+        "metric": "RF frames/s & Green terms/s: surrogate (with exact fallback at 1e-3) vs exact FP32 path",
+        "value": frames / t_sur_full, "unit": "frames/s", "n_gpus": 1, "higher_is_better": True,
+        "dtype": "bf16 weights, f32 accumulate (network); f32 exact fallback", "data": "synthetic (seeded)",
+        "config": {"workload": "cfg5: cfg1 probe; train 2M samples (x, z, f, theta) over the cfg1 box, "
+                               "fc(1 +- B/2), +-16 deg; use 1,000,000 scatterers x 75 plane waves",
+                   "train_samples": args.sur_train, "epochs": args.sur_epochs,
+                   "simus_sample_scatterers": args.sur_sample, "n_freq": int(plan.selected_freqs.shape[0])},
+        "training": {"seconds": rep["train_s"], "data_seconds": rep["data_s"], "steps": rep["steps"],
+                     "final_train_mse": rep["history"][-1]["train_mse"],
+                     "val_rel_l2": rep["history"][-1]["val_rel_l2"], "history": rep["history"]},
+        "field_rel_l2_1M_queries": val_rel,
+        "per_query_s": {"network": t_net_q, "exact_kernel": t_exact_q, "ratio_network_over_exact": t_net_q / t_exact_q},
+        "simus_1M_x75": {
+            "surrogate_s_scaled": t_sur_full, "exact_fp32_batched_s": t_exact_full,
+            "gain_vs_exact": t_exact_full / t_sur_full,
+            "fallback_fraction": res["fallback_fraction"], "tile_rel_err_median": res["tile_rel_err_median"],
+            "rf_rel_l2_vs_exact_with_fallback": res["rf_rel_l2_vs_exact"],
+            "rf_rel_l2_vs_exact_network_only": loose["rf_rel_l2_vs_exact"],
+            "network_only_s_scaled": loose["t_surrogate_total_s"] * scale,
+            "green_terms_per_s_surrogate": terms / t_sur_full, "green_terms_per_s_exact": terms / t_exact_full,
+            "frames_per_s_exact": frames / t_exact_full,
+            "breakdown_sample_s": {k: res[k] for k in ("t_network_s", "t_judge_fallback_s", "t_rx_s")},
+        },
+    }
+    return line
 
 
 def main():
@@ -643,14 +758,18 @@ def main():
     ap.add_argument("--cpu-points", type=int, default=16384)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="device timing only (profiling runs)")
+    ap.add_argument("--no-paths", action="store_true", help="skip the batched / tensor-core / surrogate summaries")
     ap.add_argument("--scatterers", type=int, default=200_000, help="smaller values make profiling cases")
     ap.add_argument("--grid-nx", type=int, default=256)
     ap.add_argument("--grid-nz", type=int, default=512)
-    ap.add_argument("--workload", choices=["cfg2", "cfg3", "cfg4"], default="cfg2",
+    ap.add_argument("--workload", choices=["cfg2", "cfg3", "cfg4", "cfg5"], default="cfg2",
                     help="cfg2: plain simus + pfield frame (default); cfg3: batched 75 waves x 16 phantoms; "
                          "cfg4: tensor-core path vs FP32 paths, 31 waves x 262,144 scatterers")
     ap.add_argument("--tc-oracle-scatterers", type=int, default=16384)
     ap.add_argument("--tc-only", action="store_true", help="cfg4 profiling case: only the tensor-core sweep")
+    ap.add_argument("--sur-train", type=int, default=2_000_000)
+    ap.add_argument("--sur-epochs", type=int, default=20)
+    ap.add_argument("--sur-sample", type=int, default=1024)
     ap.add_argument("--phantoms", type=int, default=16)
     ap.add_argument("--transmits", type=int, default=75)
     args = ap.parse_args()
@@ -658,9 +777,11 @@ def main():
     if args.impl == "reference":
         run_reference_arm(args, rank, world)
     elif args.workload == "cfg3":
-        run_batched_workload(args)
+        print(json.dumps(run_batched_workload(args)), flush=True)
     elif args.workload == "cfg4":
-        run_tc_workload(args)
+        print(json.dumps(run_tc_workload(args)), flush=True)
+    elif args.workload == "cfg5":
+        print(json.dumps(run_surrogate_workload(args)), flush=True)
     else:
         run_gpu_arm(args, rank, world)
 
