@@ -417,11 +417,74 @@ def run_gpu_arm(args, rank, world):
             "value": 1.0 / t, "unit": UNIT, "cores": cores, "kind": "port", "cpu": model,
             "sample": f"{args.cpu_scatterers} scatterers + {args.cpu_points} grid points of the frame, sharded over "
                       f"{cores} processes, scaled linearly to 200,000 scatterers + 131,072 points"}
+    if not args.no_ref_gpu and world == 1:
+        line["reference_gpu_kernel"] = reference_gpu_leg(args, device, scat, rc, delays, plan, params, medium,
+                                                         flush, simus_avg)
     if not args.no_paths and world == 1:
         line["paths"] = other_paths(args)
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def reference_gpu_leg(args, device, scat, rc, delays, plan, params, medium, flush, our_simus_ms) -> dict:
+    """The reference's own CUDA kernel (simus_fused.cu, compiled from its source for sm_103a, stock
+    launch shape) on the same frame and GPU: time per sweep (zeroed outputs + kernel, CUDA
+    events, L2 flushed), and its accuracy against this build's sweep on the full frame and
+    against the FP64 oracle on a 512-scatterer sample.  Failure is recorded, not raised."""
+    import torch
+
+    from tests._golden import max_phase_err, rel_l2
+
+    try:
+        from oracle import ref_gpu
+        import oracle.fastsimus_fp64 as O
+        from fastsimus_gb300.simus import simus_gb300
+
+        E, U, nf = params.n_elements, int(plan.n_sub), int(plan.selected_freqs.shape[0])
+        ok, why = ref_gpu.available(E, U, nf)
+        if not ok:
+            return {"unavailable": why}
+        k = ref_gpu.RefSimusKernel(E, U, nf, device)
+        d = k.prepare(scat, rc, delays, plan, params, medium)
+        re, im = k.outputs()
+        for _ in range(max(args.warmup, 2)):
+            k.launch(d, re, im)
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(max(args.steps, 3)):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            k.launch(d, re, im)
+            e.record()
+            torch.cuda.synchronize()
+            ms.append(s.elapsed_time(e))
+        t = float(np.mean(ms))
+        c128 = lambda t: t.cpu().numpy().astype(np.complex128)  # noqa: E731
+        ref_full = c128(torch.complex(re, im).reshape(E, nf).T)
+        ones = np.ones(E)
+        ours_full = c128(simus_gb300(scat, rc, params, plan, medium, delays, ones))
+        idx = np.random.default_rng(7).choice(scat.shape[0], 512, replace=False)
+        ref_s = c128(k.spectrum(scat[idx], rc[idx], delays, plan, params, medium))
+        ours_s = c128(simus_gb300(scat[idx], rc[idx], params, plan, medium, delays, ones))
+        gold = O.simus_spectrum_selected(scat[idx], rc[idx], delays, plan, params, medium)
+        k.close()
+        terms = scat.shape[0] * E * U * nf
+        return {
+            "source": "src/fast_simus/kernels/simus_fused.cu compiled by oracle/ref_gpu_build.py (nvcc sm_103a, "
+                      "--use_fast_math, the -D set and 256x128 launch of kernels/cuda_simus.py)",
+            "sweep_ms": t, "gb300_sweep_ms": our_simus_ms, "speedup_gb300_vs_reference_kernel": t / our_simus_ms,
+            "green_terms_per_s": terms / (t * 1e-3),
+            "relL2_vs_gb300_full_frame": rel_l2(ref_full, ours_full),
+            "max_phase_err_rad_vs_gb300_full_frame": max_phase_err(ref_full, ours_full),
+            "relL2_vs_fp64_oracle_512": rel_l2(ref_s, gold),
+            "max_phase_err_rad_vs_fp64_oracle_512": max_phase_err(ref_s, gold),
+            "gb300_relL2_vs_fp64_oracle_512": rel_l2(ours_s, gold),
+            "gb300_max_phase_err_rad_vs_fp64_oracle_512": max_phase_err(ours_s, gold),
+        }
+    except Exception as exc:  # recorded in the JSON line
+        return {"error": f"{type(exc).__name__}: {exc}"}
 
 
 def other_paths(args) -> dict:
@@ -758,6 +821,8 @@ def main():
     ap.add_argument("--cpu-points", type=int, default=16384)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="device timing only (profiling runs)")
+    ap.add_argument("--no-ref-gpu", action="store_true",
+                    help="skip the reference CUDA kernel leg of the default line")
     ap.add_argument("--no-paths", action="store_true", help="skip the batched / tensor-core / surrogate summaries")
     ap.add_argument("--scatterers", type=int, default=200_000, help="smaller values make profiling cases")
     ap.add_argument("--grid-nx", type=int, default=256)
