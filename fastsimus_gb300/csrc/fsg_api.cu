@@ -341,10 +341,7 @@ extern "C" int32_t fsg_pfield(const FsgProbe* probe, const FsgMedium* medium, co
   A.n_anchor = (F + kAnchor - 1) / kAnchor;
   convex_geometry(probe, &A.convex, &A.apex, &A.radius2);
   A.partial = partial;
-  cudaError_t e = cudaFuncSetAttribute(pfield_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem);
-  if ((st = check_cuda(e, "cudaFuncSetAttribute(pfield_band_kernel)")) != FSG_OK) return st;
-  pfield_band_kernel<<<dim3(c.n_bands, c.n_slices), kThreads, c.smem, s>>>(A);
-  if ((st = check_cuda(cudaGetLastError(), "pfield_band_kernel launch")) != FSG_OK) return st;
+  if ((st = check_cuda(launch_pfield_band_any(c, A, s), "pfield_band_kernel launch")) != FSG_OK) return st;
   pfield_reduce<<<(unsigned)((n_points + 255) / 256), 256, 0, s>>>(partial, c.n_bands, n_points,
                                                                   (float)plan->correction_factor, out);
   return check_cuda(cudaGetLastError(), "pfield_reduce launch");

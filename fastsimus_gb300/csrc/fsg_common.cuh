@@ -113,6 +113,19 @@ __device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 acc) {  // acc
 
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 
+// Two complex recurrences advanced at once on the packed FP32x2 pipe (sm_100+ FFMA2/FMUL2):
+// lane 0 of each float2 belongs to chain a, lane 1 to chain b, with real and imaginary parts
+// in separate pairs (gr, gi) and the steps as (sr, si, sn = -si).  Four packed instructions
+// replace eight scalar ones; each lane rounds exactly like the scalar fmaf/mul sequence.
+__device__ __forceinline__ void cstep2(float2& gr, float2& gi, float2 sr, float2 si, float2 sn) {
+  const float2 tr = __fmul2_rn(gr, sr);
+  const float2 ti = __fmul2_rn(gi, sr);
+  const float2 nr = __ffma2_rn(gi, sn, tr);  // gr sr - gi si
+  const float2 ni = __ffma2_rn(gr, si, ti);  // gr si + gi sr
+  gr = nr;
+  gi = ni;
+}
+
 // Per-sweep physical constants (kernel argument, by value).
 struct SweepConst {
   float2 dk;        // frequency-step wavenumber 2 pi df / c, double-float

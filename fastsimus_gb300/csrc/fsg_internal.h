@@ -46,7 +46,7 @@ struct BandArgs {
 
 struct SmemLayout {
   int rows, pitch;     // geometry rows (gn * kSrcPerThread) and row pitch (st + 1)
-  size_t off_rhi, off_rlo, off_amp, off_step, off_w, off_pp, off_ka, off_aa, off_da, total;
+  size_t off_rhi, off_rlo, off_amp, off_step, off_w, off_pp, off_ka, off_aa, off_da, off_y, total;
 };
 
 __host__ __device__ inline size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
@@ -67,6 +67,8 @@ __host__ __device__ inline SmemLayout smem_layout(int gn, int st, int fb, int E,
   L.off_ka = o; o = align16(o + (size_t)na * 8);
   L.off_aa = o; o = align16(o + (size_t)na * 4);
   L.off_da = o; o = align16(o + (size_t)na * E * 8);
+  // simus: each thread's running receive spectrum Y[kAnchor], laid out [j][thread]
+  L.off_y = o; o = align16(o + (with_w ? (size_t)kAnchor * kThreads * 8 : 0));
   L.total = o;
   return L;
 }
@@ -80,7 +82,8 @@ struct SweepConfig {
 __global__ void setup_tables(SetupArgs a);
 // Launches simus_band_kernel<U> (U = n_sub in 1..4) with c's grid and shared memory.
 cudaError_t launch_simus_band_any(int U, const SweepConfig& c, const BandArgs& A, cudaStream_t s);
-__global__ void pfield_band_kernel(const BandArgs A);
+// Launches pfield_band_kernel<gn> with c's grid and shared memory.
+cudaError_t launch_pfield_band_any(const SweepConfig& c, const BandArgs& A, cudaStream_t s);
 __global__ void simus_reduce(const float2* __restrict__ partial, int n_slices, int F, int E,
                              const float* __restrict__ probe, float corr, int full, int n_rows, int idx0,
                              float2* __restrict__ out);

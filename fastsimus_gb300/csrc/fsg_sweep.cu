@@ -9,11 +9,12 @@
 //   2. TX: the same thread advances its 16 transmit-weighted Green's terms through the band
 //      (re-anchored every kAnchor steps), sums them, and the `gn` threads that share a
 //      scatterer finish the sum over all E*U sources with warp shuffles.  The product
-//      rc * pulse * probe * P is the scattered field W[f][s] (simus) or |.|^2 is
+//      rc * pulse * probe * P is the scattered field W[s][f] (simus) or |.|^2 is
 //      accumulated per point (pfield);
 //   3. RX (simus): thread (element e, run of kAnchor frequencies) re-generates the receive
 //      Green's terms of every scatterer of the tile from the parked geometry and accumulates
-//      Y[e][f] += W[f][s] * mean_u G(s, e, u, f) in registers.
+//      Y[e][f] += W[s][f] * mean_u G(s, e, u, f) in registers (per tile; the running sum
+//      over tiles sits in shared memory).
 // Neither the scatterer x element Green's tile nor W ever leaves the SM; the only global
 // output is one (F x E) partial spectrum per slice, summed in a fixed order by fsg_reduce.
 
@@ -113,9 +114,13 @@ __device__ __forceinline__ void load_band_tables(const BandArgs& A, const SmemLa
 }
 
 // Geometry + TX over one band for one tile.  Each thread owns point `sl` of the tile and
-// sources [g*16, g*16+16).  `sink(f_local, psum)` is called by the thread with g == 0 once
-// per frequency with the full source sum.
-template <class Sink>
+// sources [g*16, g*16+16); the GN threads of a point are GN adjacent lanes of one warp.
+// Frequencies are processed in blocks of GN steps: every lane keeps its partial source sums
+// of the block, then a reduce-scatter across the GN lanes (log2 GN shuffle levels, halving
+// the exchanged values each level) leaves lane g with the full sum of frequency block + g.
+// `sink(f_local, psum)` is therefore called by every lane, once per block, each for its own
+// frequency.
+template <int GN, class Sink>
 __device__ __forceinline__ void tx_tile(const BandArgs& A, const SmemLayout& L, unsigned char* sm, int64_t p_idx,
                                         int sl, int g, Sink& sink) {
   float* b_rhi = reinterpret_cast<float*>(sm + L.off_rhi);
@@ -144,55 +149,84 @@ __device__ __forceinline__ void tx_tile(const BandArgs& A, const SmemLayout& L, 
       }
     }
   }
-  // 2. transmit sweep: exact anchor every kTxAnchor steps, FP32 recurrence in between
-  float2 G[kSrcPerThread];
-  float2 S[kSrcPerThread];
+  // 2. transmit sweep: exact anchor every kTxAnchor steps, FP32 recurrence in between.
+  // Sources 2p and 2p+1 of the thread's 16 share one packed FP32x2 lane pair (real and
+  // imaginary parts in separate pairs), so a step costs four packed instructions per two
+  // sources and the source sum two packed adds.
+  constexpr int kPairs = kSrcPerThread / 2;
+  float2 Gr[kPairs], Gi[kPairs], Sr[kPairs], Si[kPairs], Sn[kPairs];
   const int n_tx_anchor = (A.fb + kTxAnchor - 1) / kTxAnchor;
   for (int m = 0; m < n_tx_anchor; ++m) {
     const int am = m * (kTxAnchor / kAnchor);  // index into the band's kAnchor-spaced tables
 #pragma unroll
-    for (int i = 0; i < kSrcPerThread; ++i) {
-      const int src = g * kSrcPerThread + i;
-      G[i] = make_float2(0.f, 0.f);
-      if (m == 0) S[i] = make_float2(0.f, 0.f);
-      if (src < A.n_src) {
-        const int e = src / A.U, u = src - e * A.U;
-        const int idx = (u * A.E + e) * L.pitch + sl;
-        G[i] = cmul(anchor_value(b_rhi[idx], b_rlo[idx], b_amp[idx], ka[am], aa[am]), da[am * A.E + e]);
-        if (m == 0) S[i] = cmul(b_st[idx], A.t.dstep[e]);
+    for (int p = 0; p < kPairs; ++p) {
+      float2 gv[2], sv[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int src = g * kSrcPerThread + 2 * p + h;
+        gv[h] = make_float2(0.f, 0.f);
+        sv[h] = make_float2(0.f, 0.f);
+        if (src < A.n_src) {
+          const int e = src / A.U, u = src - e * A.U;
+          const int idx = (u * A.E + e) * L.pitch + sl;
+          gv[h] = cmul(anchor_value(b_rhi[idx], b_rlo[idx], b_amp[idx], ka[am], aa[am]), da[am * A.E + e]);
+          if (m == 0) sv[h] = cmul(b_st[idx], A.t.dstep[e]);
+        }
+      }
+      Gr[p] = make_float2(gv[0].x, gv[1].x);
+      Gi[p] = make_float2(gv[0].y, gv[1].y);
+      if (m == 0) {
+        Sr[p] = make_float2(sv[0].x, sv[1].x);
+        Si[p] = make_float2(sv[0].y, sv[1].y);
+        Sn[p] = make_float2(-sv[0].y, -sv[1].y);
       }
     }
-    const int n_steps = min(kTxAnchor, A.fb - m * kTxAnchor);
-#pragma unroll 2
-    for (int j = 0; j < n_steps; ++j) {
-      float2 ps = G[0];
-      G[0] = cmul(G[0], S[0]);
+    const int n_steps = min(kTxAnchor, A.fb - m * kTxAnchor);  // a multiple of kAnchor, so of GN
+#pragma unroll 1
+    for (int jb = 0; jb < n_steps; jb += GN) {
+      float vr[GN], vi[GN];
 #pragma unroll
-      for (int i = 1; i < kSrcPerThread; ++i) {
-        ps = cadd(ps, G[i]);
-        G[i] = cmul(G[i], S[i]);
+      for (int j = 0; j < GN; ++j) {
+        float2 ar = Gr[0], ai = Gi[0];
+        cstep2(Gr[0], Gi[0], Sr[0], Si[0], Sn[0]);
+#pragma unroll
+        for (int p = 1; p < kPairs; ++p) {
+          ar = __fadd2_rn(ar, Gr[p]);
+          ai = __fadd2_rn(ai, Gi[p]);
+          cstep2(Gr[p], Gi[p], Sr[p], Si[p], Sn[p]);
+        }
+        vr[j] = ar.x + ar.y;
+        vi[j] = ai.x + ai.y;
       }
-      for (int off = 1; off < A.gn; off <<= 1) {
-        ps.x += __shfl_xor_sync(0xffffffffu, ps.x, off);
-        ps.y += __shfl_xor_sync(0xffffffffu, ps.y, off);
+      // reduce-scatter: at level h the lane with bit h set keeps the upper half of its values
+#pragma unroll
+      for (int h = GN / 2; h >= 1; h >>= 1) {
+        const bool up = (g & h) != 0;
+#pragma unroll
+        for (int i = 0; i < h; ++i) {
+          const float sr = up ? vr[i] : vr[i + h], si = up ? vi[i] : vi[i + h];
+          const float kr = up ? vr[i + h] : vr[i], ki = up ? vi[i + h] : vi[i];
+          vr[i] = kr + __shfl_xor_sync(0xffffffffu, sr, h);
+          vi[i] = ki + __shfl_xor_sync(0xffffffffu, si, h);
+        }
       }
-      if (g == 0) sink(m * kTxAnchor + j, ps);
+      sink(m * kTxAnchor + jb + g, make_float2(vr[0], vi[0]));
     }
   }
 }
 
 struct SimusSink {
-  float2* W;        // [fb][st]
+  float2* W;        // [st][fb]
   const float2* pp; // [fb]
   float w;          // rc (0 when out of field or padding)
-  int sl, st;
+  int sl, fb;
   __device__ __forceinline__ void operator()(int fl, float2 ps) {
     float2 v = cmul(pp[fl], ps);
-    W[fl * st + sl] = make_float2(w * v.x, w * v.y);
+    W[sl * fb + fl] = make_float2(w * v.x, w * v.y);
   }
 };
 
-template <int U>
+template <int U, int GN>
 __global__ void __launch_bounds__(kThreads, 1) simus_band_kernel(const BandArgs A) {
   extern __shared__ __align__(16) unsigned char sm[];
   const SmemLayout L = smem_layout(A.gn, A.st, A.fb, A.E, true);
@@ -202,16 +236,18 @@ __global__ void __launch_bounds__(kThreads, 1) simus_band_kernel(const BandArgs 
   const int64_t s_end = min(A.n_pts, s_begin + A.per_slice);
   load_band_tables(A, L, sm, f_b0);
 
-  const int g = tid % A.gn;
-  const int sl = tid / A.gn;  // < st by construction (gn * st == 256)
+  const int g = tid % GN;
+  const int sl = tid / GN;  // < st by construction (gn * st == 256)
   const int n_runs = A.fb / kAnchor;
   const bool rx_on = tid < A.E * n_runs;
   const int e_rx = tid % A.E;
   const int run = tid / A.E;
 
-  float2 Y[kAnchor];
+  // Running receive spectrum of this thread, kept in shared memory ([j][thread]) so the
+  // registers go to the per-tile partials and the recurrence state.
+  float2* Ys = reinterpret_cast<float2*>(sm + L.off_y);
 #pragma unroll
-  for (int j = 0; j < kAnchor; ++j) Y[j] = make_float2(0.f, 0.f);
+  for (int j = 0; j < kAnchor; ++j) Ys[j * kThreads + tid] = make_float2(0.f, 0.f);
 
   float* b_rhi = reinterpret_cast<float*>(sm + L.off_rhi);
   float* b_rlo = reinterpret_cast<float*>(sm + L.off_rlo);
@@ -237,8 +273,8 @@ __global__ void __launch_bounds__(kThreads, 1) simus_band_kernel(const BandArgs 
         if (A.convex) out = out || (x * x + (z + A.apex) * (z + A.apex) <= A.radius2);
         w = out ? 0.f : (float)A.rc[si];
       }
-      SimusSink sink{W, pp, w, sl, A.st};
-      tx_tile(A, L, sm, si, sl, g, sink);
+      SimusSink sink{W, pp, w, sl, A.fb};
+      tx_tile<GN>(A, L, sm, si, sl, g, sink);
     }
     __syncthreads();
     // ---------------- RX ----------------
@@ -246,7 +282,10 @@ __global__ void __launch_bounds__(kThreads, 1) simus_band_kernel(const BandArgs 
       float2 Yt[kAnchor];
 #pragma unroll
       for (int j = 0; j < kAnchor; ++j) Yt[j] = make_float2(0.f, 0.f);
+#pragma unroll 1
       for (int s = 0; s < A.st; ++s) {
+        // this scatterer's field over my run of frequencies: contiguous, read 2 per load
+        const float4* Wrun = reinterpret_cast<const float4*>(W + s * A.fb + run * kAnchor);
         float2 Gu[U], Su[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
@@ -254,7 +293,6 @@ __global__ void __launch_bounds__(kThreads, 1) simus_band_kernel(const BandArgs 
           Gu[u] = anchor_value(b_rhi[idx], b_rlo[idx], b_amp[idx], k_run, a_run);
           Su[u] = b_st[idx];
         }
-        const float2* Wcol = W + (run * kAnchor) * A.st + s;
 #pragma unroll
         for (int j = 0; j < kAnchor; ++j) {
           float2 rp = Gu[0];
@@ -264,11 +302,12 @@ __global__ void __launch_bounds__(kThreads, 1) simus_band_kernel(const BandArgs 
             rp = cadd(rp, Gu[u]);
             Gu[u] = cmul(Gu[u], Su[u]);
           }
-          Yt[j] = cfma(Wcol[j * A.st], rp, Yt[j]);
+          const float4 w2 = Wrun[j >> 1];
+          Yt[j] = cfma((j & 1) ? make_float2(w2.z, w2.w) : make_float2(w2.x, w2.y), rp, Yt[j]);
         }
       }
 #pragma unroll
-      for (int j = 0; j < kAnchor; ++j) Y[j] = cadd(Y[j], Yt[j]);
+      for (int j = 0; j < kAnchor; ++j) Ys[j * kThreads + tid] = cadd(Ys[j * kThreads + tid], Yt[j]);
     }
     __syncthreads();
   }
@@ -277,7 +316,7 @@ __global__ void __launch_bounds__(kThreads, 1) simus_band_kernel(const BandArgs 
 #pragma unroll
     for (int j = 0; j < kAnchor; ++j) {
       int f = f_b0 + run * kAnchor + j;
-      if (f < A.F) out[(size_t)f * A.E + e_rx] = Y[j];
+      if (f < A.F) out[(size_t)f * A.E + e_rx] = Ys[j * kThreads + tid];
     }
   }
 }
@@ -294,7 +333,8 @@ struct PfieldSink {
   }
 };
 
-__global__ void __launch_bounds__(kThreads, 2) pfield_band_kernel(const BandArgs A) {
+template <int GN>
+__global__ void __launch_bounds__(kThreads, GN >= 32 ? 1 : 2) pfield_band_kernel(const BandArgs A) {
   extern __shared__ __align__(16) unsigned char sm[];
   const SmemLayout L = smem_layout(A.gn, A.st, A.fb, A.E, false);
   const int tid = threadIdx.x;
@@ -303,8 +343,8 @@ __global__ void __launch_bounds__(kThreads, 2) pfield_band_kernel(const BandArgs
   const int64_t p_end = min(A.n_pts, p_begin + A.per_slice);
   load_band_tables(A, L, sm, f_b0);
   __syncthreads();
-  const int g = tid % A.gn;
-  const int sl = tid / A.gn;
+  const int g = tid % GN;
+  const int sl = tid / GN;
   const float2* pp = reinterpret_cast<const float2*>(sm + L.off_pp);
   float* out = reinterpret_cast<float*>(A.partial) + (size_t)blockIdx.x * A.n_pts;
   for (int64_t t0 = p_begin; t0 < p_end; t0 += A.st) {
@@ -312,12 +352,16 @@ __global__ void __launch_bounds__(kThreads, 2) pfield_band_kernel(const BandArgs
     bool valid = p < p_end;
     int64_t pi = valid ? p : t0;
     PfieldSink sink{pp, 0.f, min(A.fb, A.F - f_b0)};
-    tx_tile(A, L, sm, pi, sl, g, sink);
+    tx_tile<GN>(A, L, sm, pi, sl, g, sink);
+    // each lane holds the band's |p|^2 over its own frequencies: sum the GN lanes in a fixed tree
+    float acc = sink.acc;
+#pragma unroll
+    for (int off = 1; off < GN; off <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
     if (valid && g == 0) {
       double x = A.pts[2 * pi], z = A.pts[2 * pi + 1];
       bool o = z < 0.0;
       if (A.convex) o = o || (x * x + (z + A.apex) * (z + A.apex) <= A.radius2);
-      out[pi] = o ? 0.f : sink.acc;
+      out[pi] = o ? 0.f : acc;
     }
   }
 }
@@ -348,23 +392,52 @@ __global__ void pfield_reduce(const float* __restrict__ partial, int n_bands, in
   out[i] = sqrtf(acc * corr);
 }
 
-template <int U>
+template <int U, int GN>
 static cudaError_t launch_simus_band(const SweepConfig& c, const BandArgs& A, cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(simus_band_kernel<U>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem);
+  cudaError_t e =
+      cudaFuncSetAttribute(simus_band_kernel<U, GN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem);
   if (e != cudaSuccess) return e;
-  simus_band_kernel<U><<<dim3(c.n_bands, c.n_slices), kThreads, c.smem, s>>>(A);
+  simus_band_kernel<U, GN><<<dim3(c.n_bands, c.n_slices), kThreads, c.smem, s>>>(A);
   return cudaGetLastError();
 }
 
-cudaError_t launch_simus_band_any(int U, const SweepConfig& c, const BandArgs& A, cudaStream_t s) {
-  switch (U) {
-    case 1: return launch_simus_band<1>(c, A, s);
-    case 2: return launch_simus_band<2>(c, A, s);
-    case 3: return launch_simus_band<3>(c, A, s);
-    case 4: return launch_simus_band<4>(c, A, s);
+template <int U>
+static cudaError_t launch_simus_band_gn(const SweepConfig& c, const BandArgs& A, cudaStream_t s) {
+  switch (c.gn) {
+    case 4: return launch_simus_band<U, 4>(c, A, s);
+    case 8: return launch_simus_band<U, 8>(c, A, s);
+    case 16: return launch_simus_band<U, 16>(c, A, s);
+    case 32: return launch_simus_band<U, 32>(c, A, s);
     default: return cudaErrorInvalidValue;
   }
 }
 
+cudaError_t launch_simus_band_any(int U, const SweepConfig& c, const BandArgs& A, cudaStream_t s) {
+  switch (U) {
+    case 1: return launch_simus_band_gn<1>(c, A, s);
+    case 2: return launch_simus_band_gn<2>(c, A, s);
+    case 3: return launch_simus_band_gn<3>(c, A, s);
+    case 4: return launch_simus_band_gn<4>(c, A, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <int GN>
+static cudaError_t launch_pfield_band(const SweepConfig& c, const BandArgs& A, cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(pfield_band_kernel<GN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem);
+  if (e != cudaSuccess) return e;
+  pfield_band_kernel<GN><<<dim3(c.n_bands, c.n_slices), kThreads, c.smem, s>>>(A);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pfield_band_any(const SweepConfig& c, const BandArgs& A, cudaStream_t s) {
+  switch (c.gn) {
+    case 4: return launch_pfield_band<4>(c, A, s);
+    case 8: return launch_pfield_band<8>(c, A, s);
+    case 16: return launch_pfield_band<16>(c, A, s);
+    case 32: return launch_pfield_band<32>(c, A, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
 
 }  // namespace fsg
