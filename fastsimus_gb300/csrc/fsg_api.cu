@@ -170,7 +170,44 @@ void convex_geometry(const FsgProbe* p, int* convex, double* apex, double* radiu
   }
 }
 
-SweepConfig simus_config(int E, int U, int F, int64_t n_scat, int num_sms) {
+// Padding between the sub-element planes of the geometry arrays that minimises shared-memory
+// bank conflicts of the transmit accesses: lane l of a warp touches source g + GN i of tile
+// point l / GN (g = l % GN), i.e. word u * plane + e * pitch + point.  Ties go to the smaller
+// pad; the receive reads (consecutive elements, stride pitch) are conflict-free for any pad.
+static int choose_plane_pad(int E, int U, int gn, int st) {
+  const int pitch = st + 1;
+  int best_pad = 0, best_cost = 1 << 30;
+  for (int pad = 0; pad < 32; ++pad) {
+    const int plane = E * pitch + pad;
+    int cost = 0;
+    for (int i = 0; i < kSrcPerThread; ++i) {
+      int count[32] = {0};
+      int worst = 0;
+      for (int l = 0; l < 32; ++l) {
+        const int g = l % gn, pt = l / gn, src = g + gn * i;
+        if (src >= E * U) continue;
+        const int word = (src % U) * plane + (src / U) * pitch + pt;
+        const int c = ++count[word % 32];
+        if (c > worst) worst = c;
+      }
+      cost += worst;
+    }
+    if (cost < best_cost) {
+      best_cost = cost;
+      best_pad = pad;
+    }
+  }
+  return best_pad;
+}
+
+// Geometry cache per chunk: sized to stay resident in L2 while every band's CTAs read it.
+constexpr size_t kGeoCacheBudget = size_t(48) << 20;
+
+// Simus sweep shape.  The scatterers are processed in chunks of chunk_tiles tiles; a chunk is
+// split into n_slices contiguous slices of per_slice scatterers, one CTA row per slice.
+// cache_budget bounds the geometry cache (chunk_tiles * geo_bytes) from above; a chunk holds
+// at least one tile per slice.
+SweepConfig simus_config(int E, int U, int F, int64_t n_scat, int num_sms, size_t cache_budget) {
   SweepConfig c;
   const int n_src = E * U;
   c.gn = next_pow2((n_src + kSrcPerThread - 1) / kSrcPerThread);
@@ -180,14 +217,22 @@ SweepConfig simus_config(int E, int U, int F, int64_t n_scat, int num_sms) {
   if (runs > 4) runs = 4;
   c.fb = kAnchor * runs;
   c.n_bands = (F + c.fb - 1) / c.fb;
+  c.plane_pad = choose_plane_pad(E, U, c.gn, c.st);
+  const SmemLayout L = smem_layout(c.st, c.fb, E, U, c.plane_pad, true);
+  c.smem = L.total;
+  c.geo_bytes = L.geo_bytes;
   const int64_t tiles = n_scat > 0 ? (n_scat + c.st - 1) / c.st : 1;
   int64_t slices = num_sms / c.n_bands;
   if (slices < 1) slices = 1;
   if (slices > tiles) slices = tiles;
-  const int64_t tps = (tiles + slices - 1) / slices;
+  int64_t tps = (int64_t)(cache_budget / c.geo_bytes) / slices;  // tiles per slice and chunk
+  if (tps < 1) tps = 1;
+  const int64_t tps_all = (tiles + slices - 1) / slices;
+  if (tps > tps_all) tps = tps_all;
+  c.n_slices = (int)slices;
   c.per_slice = tps * c.st;
-  c.n_slices = (int)((tiles + tps - 1) / tps);
-  c.smem = smem_layout(c.gn, c.st, c.fb, E, true).total;
+  c.chunk_tiles = tps * slices;
+  c.n_chunks = (tiles + c.chunk_tiles - 1) / c.chunk_tiles;
   return c;
 }
 
@@ -208,7 +253,8 @@ SweepConfig pfield_config(int E, int U, int F, int64_t n_pts, int num_sms) {
   const int64_t tps = (tiles + slices - 1) / slices;
   c.per_slice = tps * c.st;
   c.n_slices = (int)((tiles + tps - 1) / tps);
-  c.smem = smem_layout(c.gn, c.st, c.fb, E, false).total;
+  c.plane_pad = choose_plane_pad(E, U, c.gn, c.st);
+  c.smem = smem_layout(c.st, c.fb, E, U, c.plane_pad, false).total;
   return c;
 }
 
@@ -220,10 +266,15 @@ extern "C" int32_t fsg_abi_version(void) { return FSG_ABI_VERSION; }
 
 extern "C" const char* fsg_last_error_string(void) { return g_last_error.c_str(); }
 
+// Workspace: tables | status word | partial spectra [n_slices][F][E] | geometry cache.
+static size_t simus_ws_size(const SweepConfig& c, int E, int U, int F) {
+  return tables_bytes(E, U, F) + 256 + align256((size_t)c.n_slices * F * E * 8) +
+         align256((size_t)c.chunk_tiles * c.geo_bytes);
+}
+
 static size_t simus_ws_size(const FsgProbe* probe, const FsgFreqPlan* plan, int64_t n_scat, int num_sms) {
-  SweepConfig c = simus_config(probe->n_elements, probe->n_sub, plan->n_freq, n_scat, num_sms);
-  return tables_bytes(probe->n_elements, probe->n_sub, plan->n_freq) +
-         align256((size_t)c.n_slices * plan->n_freq * probe->n_elements * 8);
+  SweepConfig c = simus_config(probe->n_elements, probe->n_sub, plan->n_freq, n_scat, num_sms, kGeoCacheBudget);
+  return simus_ws_size(c, probe->n_elements, probe->n_sub, plan->n_freq);
 }
 
 extern "C" size_t fsg_simus_workspace_size(const FsgProbe* probe, const FsgFreqPlan* plan, int64_t n_scat) {
@@ -253,16 +304,24 @@ extern "C" int32_t fsg_simus(const FsgProbe* probe, const FsgMedium* medium, con
   int sms = 0;
   if ((st = device_sm_count(&sms)) != FSG_OK) return st;
   const int E = probe->n_elements, U = probe->n_sub, F = plan->n_freq;
-  const size_t need = simus_ws_size(probe, plan, n_scat, sms);
+  // the default chunking, or smaller chunks when the caller's workspace is smaller
+  SweepConfig c = simus_config(E, U, F, n_scat, sms, kGeoCacheBudget);
+  if (workspace && workspace_bytes < simus_ws_size(c, E, U, F)) {
+    const size_t fixed = simus_ws_size(c, E, U, F) - align256((size_t)c.chunk_tiles * c.geo_bytes);
+    if (workspace_bytes > fixed) c = simus_config(E, U, F, n_scat, sms, workspace_bytes - fixed - 256);
+  }
+  const size_t need = simus_ws_size(c, E, U, F);
   if (!workspace || workspace_bytes < need)
     return set_error(FSG_EWORKSPACE, "workspace of %zu bytes is smaller than the %zu bytes required", workspace_bytes,
                      need);
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream_ptr);
   unsigned char* ws = static_cast<unsigned char*>(workspace);
   Tables t = carve_tables(ws, E, U, F);
-  float2* partial = reinterpret_cast<float2*>(ws + tables_bytes(E, U, F));
+  int* status = reinterpret_cast<int*>(ws + tables_bytes(E, U, F));
+  float2* partial = reinterpret_cast<float2*>(ws + tables_bytes(E, U, F) + 256);
+  unsigned char* geo = reinterpret_cast<unsigned char*>(partial) + align256((size_t)c.n_slices * F * E * 8);
+  if ((st = check_cuda(cudaMemsetAsync(status, 0, sizeof(int), s), "status reset")) != FSG_OK) return st;
   if ((st = launch_setup(probe, medium, plan, delays, apod, t, s)) != FSG_OK) return st;
-  SweepConfig c = simus_config(E, U, F, n_scat, sms);
   if (n_scat > 0) {
     BandArgs A;
     A.pts = scat_xz;
@@ -275,20 +334,37 @@ extern "C" int32_t fsg_simus(const FsgProbe* probe, const FsgMedium* medium, con
     A.U = U;
     A.n_src = E * U;
     A.gn = c.gn;
+    A.plane_pad = c.plane_pad;
     A.st = c.st;
     A.fb = c.fb;
     A.F = F;
     A.n_anchor = (F + kAnchor - 1) / kAnchor;
     convex_geometry(probe, &A.convex, &A.apex, &A.radius2);
     A.partial = partial;
-    if ((st = check_cuda(launch_simus_band_any(U, c, A, s), "simus_band_kernel launch")) != FSG_OK) return st;
+    A.geo = geo;
+    A.geo_bytes = c.geo_bytes;
+    A.status = status;
+    const int64_t tiles = (n_scat + c.st - 1) / c.st;
+    for (int64_t k = 0; k < c.n_chunks; ++k) {
+      A.chunk_s0 = k * c.chunk_tiles * c.st;
+      A.accumulate = k > 0;
+      const int64_t left = tiles - k * c.chunk_tiles;
+      const int64_t ct = left < c.chunk_tiles ? left : c.chunk_tiles;
+      const int64_t items = ct * A.n_src * c.st;
+      const int64_t want = (items + 255) / 256, cap = (int64_t)sms * 16;
+      const int blocks = (int)(want < cap ? want : cap);
+      geometry_kernel<<<blocks, 256, 0, s>>>(A, ct);
+      if ((st = check_cuda(cudaGetLastError(), "geometry_kernel launch")) != FSG_OK) return st;
+      if ((st = check_cuda(launch_simus_band_any(U, c, A, s), "simus_band_kernel launch")) != FSG_OK) return st;
+    }
   }
   const int full = out_layout == FSG_OUT_FULL_CORRECTED;
   const int rows = full ? plan->n_freq_full : F;
   const int64_t n_out = (int64_t)rows * E;
   simus_reduce<<<(unsigned)((n_out + 255) / 256), 256, 0, s>>>(partial, n_scat > 0 ? c.n_slices : 0, F, E, t.probe,
                                                                full ? (float)plan->correction_factor : 1.0f, full,
-                                                               rows, plan->freq_idx_start, static_cast<float2*>(out));
+                                                               rows, plan->freq_idx_start, status,
+                                                               static_cast<float2*>(out));
   return check_cuda(cudaGetLastError(), "simus_reduce launch");
 }
 
@@ -335,6 +411,7 @@ extern "C" int32_t fsg_pfield(const FsgProbe* probe, const FsgMedium* medium, co
   A.U = U;
   A.n_src = E * U;
   A.gn = c.gn;
+  A.plane_pad = c.plane_pad;
   A.st = c.st;
   A.fb = c.fb;
   A.F = F;

@@ -39,28 +39,43 @@ struct BandArgs {
   Tables t;
   SweepConst C;
   int E, U, n_src, gn, st, fb, F, n_anchor;
+  int plane_pad;       // extra words between the sub-element planes of the geometry arrays
   int convex;
   double apex, radius2;
   void* partial;       // simus: float2 [slices][F][E]; pfield: float [bands][n_pts]
+  // simus: scatterers are processed in chunks; the geometry of a chunk's tiles is computed
+  // once by geometry_kernel into `geo` (one SmemLayout geometry block of geo_bytes per tile)
+  // and copied into shared memory by each band's CTA with a TMA bulk copy
+  unsigned char* geo;
+  size_t geo_bytes;
+  int64_t chunk_s0;    // first scatterer of the chunk (pts / rc are indexed globally)
+  int accumulate;      // add to the partial spectrum instead of overwriting it
+  int* status;         // FSG_ETIMEOUT when a bounded wait gave up
 };
 
 struct SmemLayout {
-  int rows, pitch;     // geometry rows (gn * kSrcPerThread) and row pitch (st + 1)
+  // Geometry arrays hold one value per (source, tile point): sub-element plane u, element e,
+  // point column sl at u * plane + e * pitch + sl.  pitch = st + 1 keeps the receive reads
+  // (consecutive elements) conflict-free; plane_pad spreads the transmit accesses (lanes =
+  // sources g + GN i of one or more points) over the banks.
+  int pitch, plane;
   size_t off_rhi, off_rlo, off_amp, off_step, off_w, off_pp, off_ka, off_aa, off_da, off_y, total;
+  size_t geo_bytes;    // the four geometry arrays, contiguous from offset 0
 };
 
 __host__ __device__ inline size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
 
-__host__ __device__ inline SmemLayout smem_layout(int gn, int st, int fb, int E, bool with_w) {
+__host__ __device__ inline SmemLayout smem_layout(int st, int fb, int E, int U, int plane_pad, bool with_w) {
   SmemLayout L;
-  L.rows = gn * kSrcPerThread;
   L.pitch = st + 1;
-  size_t n = (size_t)L.rows * L.pitch;
+  L.plane = E * L.pitch + plane_pad;
+  size_t n = (size_t)U * L.plane;
   size_t o = 0;
   L.off_rhi = o; o = align16(o + n * 4);
   L.off_rlo = o; o = align16(o + n * 4);
   L.off_amp = o; o = align16(o + n * 4);
   L.off_step = o; o = align16(o + n * 8);
+  L.geo_bytes = o;
   L.off_w = o; o = align16(o + (with_w ? (size_t)fb * st * 8 : 0));
   L.off_pp = o; o = align16(o + (size_t)fb * 8);
   int na = fb / kAnchor;
@@ -74,19 +89,24 @@ __host__ __device__ inline SmemLayout smem_layout(int gn, int st, int fb, int E,
 }
 
 struct SweepConfig {
-  int gn, st, fb, n_bands, n_slices;
-  int64_t per_slice;
+  int gn, st, fb, n_bands, n_slices, plane_pad;
+  int64_t per_slice;   // pfield: points per slice; simus: scatterers per slice within a chunk
+  int64_t chunk_tiles; // simus: tiles per chunk (a multiple of n_slices)
+  int64_t n_chunks;
+  size_t geo_bytes;    // simus: geometry block per tile
   size_t smem;
 };
 
 __global__ void setup_tables(SetupArgs a);
+// Geometry of every (scatterer, source) of one chunk into A.geo (tile-major SmemLayout blocks).
+__global__ void geometry_kernel(const BandArgs A, int64_t chunk_tiles);
 // Launches simus_band_kernel<U> (U = n_sub in 1..4) with c's grid and shared memory.
 cudaError_t launch_simus_band_any(int U, const SweepConfig& c, const BandArgs& A, cudaStream_t s);
 // Launches pfield_band_kernel<gn> with c's grid and shared memory.
 cudaError_t launch_pfield_band_any(const SweepConfig& c, const BandArgs& A, cudaStream_t s);
 __global__ void simus_reduce(const float2* __restrict__ partial, int n_slices, int F, int E,
                              const float* __restrict__ probe, float corr, int full, int n_rows, int idx0,
-                             float2* __restrict__ out);
+                             const int* __restrict__ status, float2* __restrict__ out);
 __global__ void pfield_reduce(const float* __restrict__ partial, int n_bands, int64_t n_pts, float corr,
                               float* __restrict__ out);
 

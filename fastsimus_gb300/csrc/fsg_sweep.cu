@@ -24,10 +24,13 @@
 
 #include "fsg_common.cuh"
 #include "fsg_internal.h"
+#include "fsg_tc.cuh"
 
 namespace fsg {
 
 constexpr double kNeperToDb = 8.685889638065035;  // 20 / ln(10)
+constexpr size_t kBulkPiece = 32 * 1024;            // bytes per TMA bulk copy instruction
+constexpr uint32_t kBulkWaitTries = 1u << 26;       // bound on the polls of one copy's mbarrier
 
 // Element / sub-element positions (utils/geometry.py:18-88, _pfield_math.py:40-67),
 // per-frequency wavenumber / attenuation / spectra, per-anchor delay-apodization factors.
@@ -113,14 +116,47 @@ __device__ __forceinline__ void load_band_tables(const BandArgs& A, const SmemLa
   }
 }
 
-// Geometry + TX over one band for one tile.  Each thread owns point `sl` of the tile and
-// sources [g*16, g*16+16); the GN threads of a point are GN adjacent lanes of one warp.
-// Frequencies are processed in blocks of GN steps: every lane keeps its partial source sums
-// of the block, then a reduce-scatter across the GN lanes (log2 GN shuffle levels, halving
-// the exchanged values each level) leaves lane g with the full sum of frequency block + g.
-// `sink(f_local, psum)` is therefore called by every lane, once per block, each for its own
-// frequency.
-template <int GN, class Sink>
+// Geometry of one (point, source) into the four geometry arrays at word index idx.
+__device__ __forceinline__ void store_geometry(float* rhi, float* rlo, float* amp, float2* stp, int idx, dfl xs, dfl zs,
+                                               const BandArgs& A, int src) {
+  const int e = src / A.U;
+  const SrcGeo geo = source_geometry(xs, zs, A.t.src_pos[src], A.t.rot_e[e], A.C);
+  rhi[idx] = geo.r_hi;
+  rlo[idx] = geo.r_lo;
+  amp[idx] = geo.amp;
+  stp[idx] = geo.step;
+}
+
+// Geometry of a chunk's tiles, once per (scatterer, source) for all frequency bands.  One
+// thread per (tile, source, point); consecutive threads take consecutive points, so the
+// writes of a warp are contiguous.  Points past the end of the scatterer list repeat the
+// tile's first point (their rc is 0 in the band kernel).
+__global__ void geometry_kernel(const BandArgs A, int64_t chunk_tiles) {
+  const SmemLayout L = smem_layout(A.st, A.fb, A.E, A.U, A.plane_pad, true);
+  const int64_t n_items = chunk_tiles * A.n_src * A.st;
+  for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < n_items;
+       it += (int64_t)gridDim.x * blockDim.x) {
+    const int pt = (int)(it % A.st);
+    const int src = (int)((it / A.st) % A.n_src);
+    const int64_t tile = it / ((int64_t)A.st * A.n_src);
+    int64_t s = A.chunk_s0 + tile * A.st + pt;
+    if (s >= A.n_pts) s = A.chunk_s0 + tile * A.st;
+    unsigned char* blk = A.geo + tile * A.geo_bytes;
+    const int e = src / A.U, u = src - e * A.U;
+    store_geometry(reinterpret_cast<float*>(blk + L.off_rhi), reinterpret_cast<float*>(blk + L.off_rlo),
+                   reinterpret_cast<float*>(blk + L.off_amp), reinterpret_cast<float2*>(blk + L.off_step),
+                   u * L.plane + e * L.pitch + pt, load_coord(A.pts + 2 * s), load_coord(A.pts + 2 * s + 1), A, src);
+  }
+}
+
+// TX over one band for one tile (with the tile's geometry computed here first when kGeo).
+// Each thread owns point `sl` of the tile and sources g + GN i (i < 16); the GN threads of a
+// point are GN adjacent lanes of one warp.  Frequencies are processed in blocks of GN steps:
+// every lane keeps its partial source sums of the block, then a reduce-scatter across the GN
+// lanes (log2 GN shuffle levels, halving the exchanged values each level) leaves lane g with
+// the full sum of frequency block + g.  `sink(f_local, psum)` is therefore called by every
+// lane, once per block, each for its own frequency.
+template <int GN, bool kGeo, class Sink>
 __device__ __forceinline__ void tx_tile(const BandArgs& A, const SmemLayout& L, unsigned char* sm, int64_t p_idx,
                                         int sl, int g, Sink& sink) {
   float* b_rhi = reinterpret_cast<float*>(sm + L.off_rhi);
@@ -132,25 +168,20 @@ __device__ __forceinline__ void tx_tile(const BandArgs& A, const SmemLayout& L, 
   const float2* da = reinterpret_cast<const float2*>(sm + L.off_da);
 
   // 1. geometry of my sources, parked in shared memory (rolled loop: one copy of the code)
-  {
+  if constexpr (kGeo) {
     const dfl xs = load_coord(A.pts + 2 * p_idx);
     const dfl zs = load_coord(A.pts + 2 * p_idx + 1);
 #pragma unroll 1
     for (int i = 0; i < kSrcPerThread; ++i) {
-      const int src = g * kSrcPerThread + i;
+      const int src = g + GN * i;
       if (src < A.n_src) {
         const int e = src / A.U, u = src - e * A.U;
-        const int idx = (u * A.E + e) * L.pitch + sl;
-        const SrcGeo geo = source_geometry(xs, zs, A.t.src_pos[src], A.t.rot_e[e], A.C);
-        b_rhi[idx] = geo.r_hi;
-        b_rlo[idx] = geo.r_lo;
-        b_amp[idx] = geo.amp;
-        b_st[idx] = geo.step;
+        store_geometry(b_rhi, b_rlo, b_amp, b_st, u * L.plane + e * L.pitch + sl, xs, zs, A, src);
       }
     }
   }
   // 2. transmit sweep: exact anchor every kTxAnchor steps, FP32 recurrence in between.
-  // Sources 2p and 2p+1 of the thread's 16 share one packed FP32x2 lane pair (real and
+  // The thread's sources i = 2p and 2p+1 share one packed FP32x2 lane pair (real and
   // imaginary parts in separate pairs), so a step costs four packed instructions per two
   // sources and the source sum two packed adds.
   constexpr int kPairs = kSrcPerThread / 2;
@@ -163,12 +194,12 @@ __device__ __forceinline__ void tx_tile(const BandArgs& A, const SmemLayout& L, 
       float2 gv[2], sv[2];
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
-        const int src = g * kSrcPerThread + 2 * p + h;
+        const int src = g + GN * (2 * p + h);
         gv[h] = make_float2(0.f, 0.f);
         sv[h] = make_float2(0.f, 0.f);
         if (src < A.n_src) {
           const int e = src / A.U, u = src - e * A.U;
-          const int idx = (u * A.E + e) * L.pitch + sl;
+          const int idx = u * L.plane + e * L.pitch + sl;
           gv[h] = cmul(anchor_value(b_rhi[idx], b_rlo[idx], b_amp[idx], ka[am], aa[am]), da[am * A.E + e]);
           if (m == 0) sv[h] = cmul(b_st[idx], A.t.dstep[e]);
         }
@@ -229,12 +260,19 @@ struct SimusSink {
 template <int U, int GN>
 __global__ void __launch_bounds__(kThreads, 1) simus_band_kernel(const BandArgs A) {
   extern __shared__ __align__(16) unsigned char sm[];
-  const SmemLayout L = smem_layout(A.gn, A.st, A.fb, A.E, true);
+  const SmemLayout L = smem_layout(A.st, A.fb, A.E, A.U, A.plane_pad, true);
+  __shared__ uint64_t s_mbar;
+  __shared__ int s_fail;
   const int tid = threadIdx.x;
   const int f_b0 = blockIdx.x * A.fb;
-  const int64_t s_begin = (int64_t)blockIdx.y * A.per_slice;
+  const int64_t s_begin = A.chunk_s0 + (int64_t)blockIdx.y * A.per_slice;
   const int64_t s_end = min(A.n_pts, s_begin + A.per_slice);
   load_band_tables(A, L, sm, f_b0);
+  if (tid == 0) {
+    tc::mbar_init(&s_mbar, 1);
+    tc::fence_mbar_init();
+    s_fail = 0;
+  }
 
   const int g = tid % GN;
   const int sl = tid / GN;  // < st by construction (gn * st == 256)
@@ -260,8 +298,24 @@ __global__ void __launch_bounds__(kThreads, 1) simus_band_kernel(const BandArgs 
   const float2 k_run = A.t.kf[min(f_b0 + (rx_on ? run : 0) * kAnchor, A.F - 1)];
   const float a_run = A.t.af[min(f_b0 + (rx_on ? run : 0) * kAnchor, A.F - 1)];
 
+  uint32_t phase = 0;
   for (int64_t t0 = s_begin; t0 < s_end; t0 += A.st) {
-    // ---------------- geometry + TX ----------------
+    // ---------------- geometry: TMA bulk copy of the tile's block ----------------
+    // The previous tile's reads of these arrays finished at the barrier that closed it; the
+    // proxy fence orders them before the asynchronous writes.  Thread 0 waits (bounded) and
+    // the barrier publishes the data and the outcome to the CTA.
+    if (tid == 0) {
+      const unsigned char* src = A.geo + ((t0 - A.chunk_s0) / A.st) * A.geo_bytes;
+      tc::fence_proxy_async_smem();
+      tc::mbar_arrive_expect_tx(&s_mbar, (uint32_t)A.geo_bytes);
+      for (size_t off = 0; off < A.geo_bytes; off += kBulkPiece)
+        tc::bulk_g2s(sm + off, src + off, (uint32_t)min(kBulkPiece, A.geo_bytes - off), &s_mbar);
+      if (!tc::mbar_wait_bounded(&s_mbar, phase, kBulkWaitTries)) s_fail = 1;
+    }
+    phase ^= 1u;
+    __syncthreads();
+    if (s_fail) break;
+    // ---------------- TX ----------------
     {
       int64_t s = t0 + sl;
       bool valid = s < s_end;
@@ -274,7 +328,7 @@ __global__ void __launch_bounds__(kThreads, 1) simus_band_kernel(const BandArgs 
         w = out ? 0.f : (float)A.rc[si];
       }
       SimusSink sink{W, pp, w, sl, A.fb};
-      tx_tile<GN>(A, L, sm, si, sl, g, sink);
+      tx_tile<GN, false>(A, L, sm, si, sl, g, sink);
     }
     __syncthreads();
     // ---------------- RX ----------------
@@ -283,27 +337,36 @@ __global__ void __launch_bounds__(kThreads, 1) simus_band_kernel(const BandArgs 
 #pragma unroll
       for (int j = 0; j < kAnchor; ++j) Yt[j] = make_float2(0.f, 0.f);
 #pragma unroll 1
-      for (int s = 0; s < A.st; ++s) {
-        // this scatterer's field over my run of frequencies: contiguous, read 2 per load
-        const float4* Wrun = reinterpret_cast<const float4*>(W + s * A.fb + run * kAnchor);
-        float2 Gu[U], Su[U];
+      // two scatterers per pass (st is even): independent recurrences give the scheduler two
+      // chains per sub-element to interleave; both accumulate into the same partial
+      for (int s = 0; s < A.st; s += 2) {
+        // the scatterers' fields over my run of frequencies: contiguous, read 2 per load
+        const float4* Wa = reinterpret_cast<const float4*>(W + s * A.fb + run * kAnchor);
+        const float4* Wb = reinterpret_cast<const float4*>(W + (s + 1) * A.fb + run * kAnchor);
+        float2 Ga[U], Sa[U], Gb[U], Sb[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-          const int idx = (u * A.E + e_rx) * L.pitch + s;
-          Gu[u] = anchor_value(b_rhi[idx], b_rlo[idx], b_amp[idx], k_run, a_run);
-          Su[u] = b_st[idx];
+          const int idx = u * L.plane + e_rx * L.pitch + s;
+          Ga[u] = anchor_value(b_rhi[idx], b_rlo[idx], b_amp[idx], k_run, a_run);
+          Sa[u] = b_st[idx];
+          Gb[u] = anchor_value(b_rhi[idx + 1], b_rlo[idx + 1], b_amp[idx + 1], k_run, a_run);
+          Sb[u] = b_st[idx + 1];
         }
 #pragma unroll
         for (int j = 0; j < kAnchor; ++j) {
-          float2 rp = Gu[0];
-          Gu[0] = cmul(Gu[0], Su[0]);
+          float2 ra = Ga[0], rb = Gb[0];
+          Ga[0] = cmul(Ga[0], Sa[0]);
+          Gb[0] = cmul(Gb[0], Sb[0]);
 #pragma unroll
           for (int u = 1; u < U; ++u) {
-            rp = cadd(rp, Gu[u]);
-            Gu[u] = cmul(Gu[u], Su[u]);
+            ra = cadd(ra, Ga[u]);
+            rb = cadd(rb, Gb[u]);
+            Ga[u] = cmul(Ga[u], Sa[u]);
+            Gb[u] = cmul(Gb[u], Sb[u]);
           }
-          const float4 w2 = Wrun[j >> 1];
-          Yt[j] = cfma((j & 1) ? make_float2(w2.z, w2.w) : make_float2(w2.x, w2.y), rp, Yt[j]);
+          const float4 wa = Wa[j >> 1], wb = Wb[j >> 1];
+          Yt[j] = cfma((j & 1) ? make_float2(wa.z, wa.w) : make_float2(wa.x, wa.y), ra, Yt[j]);
+          Yt[j] = cfma((j & 1) ? make_float2(wb.z, wb.w) : make_float2(wb.x, wb.y), rb, Yt[j]);
         }
       }
 #pragma unroll
@@ -311,12 +374,17 @@ __global__ void __launch_bounds__(kThreads, 1) simus_band_kernel(const BandArgs 
     }
     __syncthreads();
   }
+  if (s_fail && tid == 0) atomicExch(A.status, FSG_ETIMEOUT);
   if (rx_on) {
     float2* out = reinterpret_cast<float2*>(A.partial) + (size_t)blockIdx.y * A.F * A.E;
 #pragma unroll
     for (int j = 0; j < kAnchor; ++j) {
       int f = f_b0 + run * kAnchor + j;
-      if (f < A.F) out[(size_t)f * A.E + e_rx] = Ys[j * kThreads + tid];
+      if (f < A.F) {
+        const float2 y = Ys[j * kThreads + tid];
+        float2* o = out + (size_t)f * A.E + e_rx;
+        *o = A.accumulate ? cadd(*o, y) : y;
+      }
     }
   }
 }
@@ -336,7 +404,7 @@ struct PfieldSink {
 template <int GN>
 __global__ void __launch_bounds__(kThreads, GN >= 32 ? 1 : 2) pfield_band_kernel(const BandArgs A) {
   extern __shared__ __align__(16) unsigned char sm[];
-  const SmemLayout L = smem_layout(A.gn, A.st, A.fb, A.E, false);
+  const SmemLayout L = smem_layout(A.st, A.fb, A.E, A.U, A.plane_pad, false);
   const int tid = threadIdx.x;
   const int f_b0 = blockIdx.x * A.fb;
   const int64_t p_begin = (int64_t)blockIdx.y * A.per_slice;
@@ -352,7 +420,7 @@ __global__ void __launch_bounds__(kThreads, GN >= 32 ? 1 : 2) pfield_band_kernel
     bool valid = p < p_end;
     int64_t pi = valid ? p : t0;
     PfieldSink sink{pp, 0.f, min(A.fb, A.F - f_b0)};
-    tx_tile<GN>(A, L, sm, pi, sl, g, sink);
+    tx_tile<GN, true>(A, L, sm, pi, sl, g, sink);
     // each lane holds the band's |p|^2 over its own frequencies: sum the GN lanes in a fixed tree
     float acc = sink.acc;
 #pragma unroll
@@ -369,9 +437,13 @@ __global__ void __launch_bounds__(kThreads, GN >= 32 ? 1 : 2) pfield_band_kernel
 // out (layout) = probe_f * corr * sum over slices of partial[q][f][e], fixed slice order.
 __global__ void simus_reduce(const float2* __restrict__ partial, int n_slices, int F, int E,
                              const float* __restrict__ probe, float corr, int full, int n_rows, int idx0,
-                             float2* __restrict__ out) {
+                             const int* __restrict__ status, float2* __restrict__ out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (int64_t)n_rows * E) return;
+  if (*status != FSG_OK) {  // a sweep CTA gave up waiting: make the failure visible in the output
+    out[i] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+    return;
+  }
   const int row = (int)(i / E), e = (int)(i % E);
   const int f = full ? row - idx0 : row;
   float2 acc = make_float2(0.f, 0.f);
