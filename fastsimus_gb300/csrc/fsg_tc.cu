@@ -53,43 +53,38 @@ struct TcArgs {
   float2* partial;  // [n_items][fb][kTcTx][kTcE]
 };
 
-// Geometry for the tensor-core path (accuracy target 1e-3): double-float distance and anchor
-// phase as in the plain kernels, but the square root comes from one rsqrt plus a correction,
-// and the recurrence step uses the MUFU sin/cos/exp2 -- its ~4e-7 error compounds over at most
-// six steps.
-__device__ __forceinline__ void tc_source(dfl xs, dfl zs, float4 sp, float2 rot, const SweepConst& C, float2 k0,
+// Geometry for the tensor-core path (accuracy target 1e-3), in plain FP32 and without
+// branches so that a thread's eight staged states overlap: distance from one rsqrt, anchor
+// phase k0 r reduced mod 2 pi in FP32 (error ~1e-7 |k0 r|, below 1e-4 rad here), MUFU
+// sin/cos/exp for the anchor and for the recurrence step (whose ~4e-7 error compounds over at
+// most six steps).  Obliquity, the 1e-16 horizon floor, the centre-frequency sinc and the
+// lambda/2 clip follow _pfield_math.py:70-118 and :165-199 as in the plain kernels.
+__device__ __forceinline__ void tc_source(float xs, float zs, float4 sp, float2 rot, const SweepConst& C, float2 k0,
                                           float a0, float2& g, float2& st) {
-  const dfl dx = df_add(xs, dfl{-sp.x, -sp.y});
-  const dfl dz = df_add(zs, dfl{-sp.z, -sp.w});
-  const dfl d2 = df_add(df_sqr(dx), df_sqr(dz));
-  float r_hi, r_lo, rinv;
-  if (d2.hi > 0.0f) {
-    rinv = rsqrtf(d2.hi);
-    const float r0 = d2.hi * rinv;
-    const float res = __fadd_rn(fmaf(-r0, r0, d2.hi), d2.lo);  // d2 - r0^2
-    const dfl r = fast_two_sum(r0, res * (0.5f * rinv));
-    r_hi = r.hi;
-    r_lo = r.lo;
-  } else {
-    r_hi = r_lo = 0.0f;
-    rinv = 0.0f;
-  }
-  float a = (r_hi > 0.0f) ? dx.hi * rinv : 1.0f;
-  a = fminf(1.0f, fmaxf(-1.0f, a));
-  const float ca = sqrtf((1.0f - a) * (1.0f + a));
+  const float dx = __fsub_rn(__fsub_rn(xs, sp.x), sp.y);
+  const float dz = __fsub_rn(__fsub_rn(zs, sp.z), sp.w);
+  const float d2 = fmaf(dx, dx, dz * dz);
+  const float rinv = rsqrtf(fmaxf(d2, 1e-30f));
+  const float r = d2 * rinv;
+  const float a = (d2 > 0.0f) ? fminf(1.0f, fmaxf(-1.0f, dx * rinv)) : 1.0f;
+  const float ca = sqrtf(fmaxf(0.0f, (1.0f - a) * (1.0f + a)));
   const float sth = fmaf(a, rot.x, -ca * rot.y);
   const float cth = fmaf(ca, rot.x, a * rot.y);
-  if (r_hi < C.min_dist.x || (r_hi == C.min_dist.x && r_lo < C.min_dist.y)) {
-    r_hi = C.min_dist.x;
-    r_lo = C.min_dist.y;
-  }
+  const float rc = fmaxf(r, C.min_dist.x);
   float ob = (C.baffle == 0) ? cth : ((C.baffle == 1) ? 1.0f : __fdividef(cth, cth + C.baffle_val));
-  if (cth <= 0.0f) ob = 1e-16f;
-  const float amp = ob * sinc_rad(C.dir_coef * sth) * rsqrtf(r_hi) * C.inv_nsub;
-  g = anchor_value(r_hi, r_lo, amp, k0, a0);
+  ob = (cth <= 0.0f) ? 1e-16f : ob;
+  const float x = C.dir_coef * sth;
+  const float dir = (fabsf(x) < 1e-4f) ? 1.0f : __fdividef(__sinf(x), x);
+  const float amp = ob * dir * rsqrtf(rc) * C.inv_nsub;
+  const float p = k0.x * rc;
+  const float n = rintf(p * kInvTwoPi);
+  const float ph = fmaf(-n, kTwoPiLo, fmaf(-n, kTwoPiHi, p));
   float sn, cs;
-  __sincosf(C.dk.x * r_hi, &sn, &cs);
-  const float mag = __expf(-C.dalpha * r_hi);
+  __sincosf(ph, &sn, &cs);
+  const float m = amp * __expf(-a0 * rc);
+  g = make_float2(m * cs, m * sn);
+  __sincosf(C.dk.x * rc, &sn, &cs);
+  const float mag = __expf(-C.dalpha * rc);
   st = make_float2(mag * cs, mag * sn);
 }
 
@@ -222,17 +217,19 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
       float2 G[16 * U], S[16 * U];
       {
         const int64_t si = sval ? s : t0;
-        const dfl xs = split_double(P.scat[2 * si]);
-        const dfl zs = split_double(P.scat[2 * si + 1]);
+        const float xs = (float)P.scat[2 * si];
+        const float zs = (float)P.scat[2 * si + 1];
 #pragma unroll
         for (int c = 0; c < 2 * U; ++c) {
-#pragma unroll 1
+#pragma unroll 4
           for (int i = 0; i < 8; ++i) {
             const int idx = c * 8 + i;  // state index j * U + u
             const int e = eg * 16 + idx / U, u = idx % U;
-            float2 g = make_float2(0.f, 0.f), st = make_float2(0.f, 0.f);
-            if (sval && e < E) tc_source(xs, zs, A.src_pos[e * U + u], A.rot_e[e], C, k0, a0, g, st);
-            stage[i * kThreads + tid] = make_float4(g.x, g.y, st.x, st.y);
+            const int ec = e < E ? e : E - 1;
+            float2 g, st;
+            tc_source(xs, zs, A.src_pos[ec * U + u], A.rot_e[ec], C, k0, a0, g, st);
+            const bool on = sval && e < E;
+            stage[i * kThreads + tid] = on ? make_float4(g.x, g.y, st.x, st.y) : make_float4(0.f, 0.f, 0.f, 0.f);
           }
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
