@@ -350,10 +350,9 @@ extern "C" int32_t fsg_simus(const FsgProbe* probe, const FsgMedium* medium, con
       A.accumulate = k > 0;
       const int64_t left = tiles - k * c.chunk_tiles;
       const int64_t ct = left < c.chunk_tiles ? left : c.chunk_tiles;
-      const int64_t items = ct * A.n_src * c.st;
-      const int64_t want = (items + 255) / 256, cap = (int64_t)sms * 16;
-      const int blocks = (int)(want < cap ? want : cap);
-      geometry_kernel<<<blocks, 256, 0, s>>>(A, ct);
+      const int64_t cap = (int64_t)sms * 8;
+      const int blocks = (int)(ct < cap ? ct : cap);
+      geometry_kernel<<<blocks, kThreads, 0, s>>>(A, ct);
       if ((st = check_cuda(cudaGetLastError(), "geometry_kernel launch")) != FSG_OK) return st;
       if ((st = check_cuda(launch_simus_band_any(U, c, A, s), "simus_band_kernel launch")) != FSG_OK) return st;
     }

@@ -63,6 +63,7 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
   float2* W = D + FB * kBE * kWPitch;                                // [kBT][kWPitch]
   float* rcs = reinterpret_cast<float*>(W + kBT * kWPitch);          // [kBT]
   __shared__ int s_item;
+  __shared__ float4 xz[kBT];  // the tile's scatterer coordinates as double-float (x hi, x lo, z hi, z lo)
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wm = warp & 3, wn = warp >> 2, lm = lane & 3, ln = lane >> 2;
@@ -120,6 +121,23 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
         for (int j = 0; j < 5; ++j) Y[f][i][j] = make_float2(0.f, 0.f);
 
     for (int64_t t0 = s_begin; t0 < s_end; t0 += kBT) {
+      // --- the tile's coordinates (split once per scatterer) and reflectivities ---
+      if (tid < kBT) {
+        const int64_t s = t0 + tid;
+        float w = 0.f;
+        float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (s < s_end) {
+          const double x = P.scat[2 * s], z = P.scat[2 * s + 1];
+          const dfl hx = split_double(x), hz = split_double(z);
+          c = make_float4(hx.hi, hx.lo, hz.hi, hz.lo);
+          bool out = z < 0.0;
+          if (A.convex) out = out || (x * x + (z + A.apex) * (z + A.apex) <= A.radius2);
+          w = out ? 0.f : (float)P.rc[s];
+        }
+        xz[tid] = c;
+        rcs[tid] = w;
+      }
+      __syncthreads();
       // --- Green's matrix Gm[f][s][e] for the tile: thread (e, s-group of 16) ---
       {
         const int e = tid & 63;
@@ -129,8 +147,8 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
           const int64_t s = t0 + sl;
           float2 g0 = make_float2(0.f, 0.f), g1 = make_float2(0.f, 0.f);
           if (e < E && s < s_end) {
-            const dfl xs = split_double(P.scat[2 * s]);
-            const dfl zs = split_double(P.scat[2 * s + 1]);
+            const float4 c = xz[sl];
+            const dfl xs{c.x, c.y}, zs{c.z, c.w};
             const float2 rot = A.rot_e[e];
             for (int u = 0; u < U; ++u) {
               const int src = e * U + u;
@@ -142,16 +160,6 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
           }
           Gm[sl * kGmPitch + e] = g0;
           if (FB > 1) Gm[(kBT + sl) * kGmPitch + e] = g1;
-          if (e == 0) {
-            float w = 0.f;
-            if (s < s_end) {
-              const double x = P.scat[2 * s], z = P.scat[2 * s + 1];
-              bool out = z < 0.0;
-              if (A.convex) out = out || (x * x + (z + A.apex) * (z + A.apex) <= A.radius2);
-              w = out ? 0.f : (float)P.rc[s];
-            }
-            rcs[sl] = w;
-          }
         }
       }
       __syncthreads();

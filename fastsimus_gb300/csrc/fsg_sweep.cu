@@ -127,25 +127,35 @@ __device__ __forceinline__ void store_geometry(float* rhi, float* rlo, float* am
   stp[idx] = geo.step;
 }
 
-// Geometry of a chunk's tiles, once per (scatterer, source) for all frequency bands.  One
-// thread per (tile, source, point); consecutive threads take consecutive points, so the
-// writes of a warp are contiguous.  Points past the end of the scatterer list repeat the
-// tile's first point (their rc is 0 in the band kernel).
-__global__ void geometry_kernel(const BandArgs A, int64_t chunk_tiles) {
+// Geometry of a chunk's tiles, once per (scatterer, source) for all frequency bands.  A CTA
+// takes one tile at a time: its scatterers' coordinates are split into double-float pairs
+// once, then thread i handles (source, point) items i, i + 256, ...; consecutive threads take
+// consecutive points, so the writes of a warp are contiguous.  Points past the end of the
+// scatterer list repeat the tile's first point (their rc is 0 in the band kernel).
+__global__ void __launch_bounds__(kThreads) geometry_kernel(const BandArgs A, int64_t chunk_tiles) {
+  __shared__ float4 xz[kThreads];  // st <= 64 points of the tile
   const SmemLayout L = smem_layout(A.st, A.fb, A.E, A.U, A.plane_pad, true);
-  const int64_t n_items = chunk_tiles * A.n_src * A.st;
-  for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < n_items;
-       it += (int64_t)gridDim.x * blockDim.x) {
-    const int pt = (int)(it % A.st);
-    const int src = (int)((it / A.st) % A.n_src);
-    const int64_t tile = it / ((int64_t)A.st * A.n_src);
-    int64_t s = A.chunk_s0 + tile * A.st + pt;
-    if (s >= A.n_pts) s = A.chunk_s0 + tile * A.st;
+  const int items = A.n_src * A.st;
+  for (int64_t tile = blockIdx.x; tile < chunk_tiles; tile += gridDim.x) {
+    __syncthreads();
+    if (threadIdx.x < A.st) {
+      int64_t s = A.chunk_s0 + tile * A.st + threadIdx.x;
+      if (s >= A.n_pts) s = A.chunk_s0 + tile * A.st;
+      const dfl hx = load_coord(A.pts + 2 * s), hz = load_coord(A.pts + 2 * s + 1);
+      xz[threadIdx.x] = make_float4(hx.hi, hx.lo, hz.hi, hz.lo);
+    }
+    __syncthreads();
     unsigned char* blk = A.geo + tile * A.geo_bytes;
-    const int e = src / A.U, u = src - e * A.U;
-    store_geometry(reinterpret_cast<float*>(blk + L.off_rhi), reinterpret_cast<float*>(blk + L.off_rlo),
-                   reinterpret_cast<float*>(blk + L.off_amp), reinterpret_cast<float2*>(blk + L.off_step),
-                   u * L.plane + e * L.pitch + pt, load_coord(A.pts + 2 * s), load_coord(A.pts + 2 * s + 1), A, src);
+    float* rhi = reinterpret_cast<float*>(blk + L.off_rhi);
+    float* rlo = reinterpret_cast<float*>(blk + L.off_rlo);
+    float* amp = reinterpret_cast<float*>(blk + L.off_amp);
+    float2* stp = reinterpret_cast<float2*>(blk + L.off_step);
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+      const int pt = it % A.st, src = it / A.st;
+      const int e = src / A.U, u = src - e * A.U;
+      const float4 c = xz[pt];
+      store_geometry(rhi, rlo, amp, stp, u * L.plane + e * L.pitch + pt, dfl{c.x, c.y}, dfl{c.z, c.w}, A, src);
+    }
   }
 }
 

@@ -135,8 +135,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
   float* X = reinterpret_cast<float*>(sm + kOffX);
   float4* stage = reinterpret_cast<float4*>(sm + kOffAtxHi);  // geometry staging (A_tx region)
 
-  // generation mapping: scatterer s_g of the tile, elements [16 eg, 16 eg + 16)
-  const int s_g = tid >> 2, eg = tid & 3;
+  // generation mapping: scatterer s_g of the tile, elements [16 eg, 16 eg + 16).  The eight
+  // lanes of a quarter-warp share eg and take eight consecutive scatterers, so their 16-byte
+  // stores into the core-matrix operand layouts fill one contiguous 128-byte row of banks.
+  const int s_g = (tid >> 5) * 8 + (tid & 7), eg = (tid >> 3) & 3;
   // TMEM read mapping: lane quarter q (rows 32q..32q+31), column half h
   const int q = warp & 3, h = warp >> 2;
 
