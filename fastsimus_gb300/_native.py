@@ -102,6 +102,10 @@ _SIGNATURES = {
     "fsg_simus_noalloc_scratch_bytes": (ctypes.c_size_t, []),
     "fsg_fp32_fma_probe": (ctypes.c_int32, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
                                             _P]),
+    "fsg_rf_workspace_size": (ctypes.c_size_t, [ctypes.c_int32, ctypes.c_int32]),
+    "fsg_irfft_gate": (ctypes.c_int32, [_P, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+                                        ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P,
+                                        ctypes.c_size_t, _P]),
 }
 
 _lib = None

@@ -8,8 +8,8 @@ and output layout, but computes every (phantom, firing) in a single launch: each
 is generated once and contracted with all firings.
 
 ``BatchedSimus`` keeps inputs, plans, workspace and outputs resident for repeated runs,
-captures the whole batch (set-up, persistent sweep, reduction, cuFFT irfft, gate) in a CUDA
-graph, and picks tile shapes with ``autotune``.
+captures the whole batch (set-up, persistent sweep, reduction, irfft + gate epilogue) in a
+CUDA graph, and picks tile shapes with ``autotune``.
 """
 
 from __future__ import annotations
@@ -53,14 +53,6 @@ def shared_plan(scatterers, rc, delays_list, params: TransducerParams, medium: M
     span (tests/_picmus_phantom_shared.py:329-347)."""
     spans = [float(np.ptp(np.nan_to_num(np.asarray(d, dtype=np.float64)))) for d in delays_list]
     return simus_precompute(scatterers, rc, delays_list[int(np.argmax(spans))], params, medium, **plan_kw)
-
-
-def _gate(rf: torch.Tensor) -> torch.Tensor:
-    """Smooth -100 dB gate of simus.py:359-365, with each firing's own peak (rf: T x N x E)."""
-    th = 1e-5
-    mag = rf.abs()
-    rel = mag / (mag.amax(dim=(1, 2), keepdim=True) + 1e-30)
-    return rf * (0.5 * (1.0 + torch.tanh((rel - th) / (th / 10.0))))
 
 
 class BatchedSimus:
@@ -151,10 +143,23 @@ class BatchedSimus:
         return int(out.value)
 
     def _finish(self):
-        self.rfs = []
-        for plan, out in zip(self.plans, self.outs):
-            rf = torch.fft.irfft(torch.conj(out), n=plan.n_fft, dim=1)[:, : (plan.n_fft + 1) // 2]
-            self.rfs.append(_gate(rf))
+        """RF of every firing: ``fsg_irfft_gate`` over each phantom's (n_tx, n_freq_full, E)
+        spectra, each firing gated with its own peak.  Buffers persist across calls, so a CUDA
+        graph that captured this keeps writing into ``self.rfs``."""
+        lib = _native.load()
+        if getattr(self, "_rf_bufs", None) is None:
+            E = self.params.n_elements
+            self._rf_bufs = [torch.empty((self.n_tx, (p.n_fft + 1) // 2, E), dtype=torch.float32, device=self.device)
+                             for p in self.plans]
+            self._rf_ws = [_device.workspace(lib.fsg_rf_workspace_size(int(p.n_fft), self.n_tx), self.device)
+                           for p in self.plans]
+        stream = _device.stream_handle(self.device)
+        for plan, out, rf, ws in zip(self.plans, self.outs, self._rf_bufs, self._rf_ws):
+            n_full, E = out.shape[1], out.shape[2]
+            _native.check(lib.fsg_irfft_gate(out.data_ptr(), self.n_tx, n_full * E, n_full, E, int(plan.n_fft),
+                                             int(plan.freq_idx_start), int(plan.selected_freqs.shape[0]), 1,
+                                             rf.data_ptr(), ws.data_ptr(), ws.numel(), stream))
+        self.rfs = self._rf_bufs
 
     def run(self) -> list[SimusResult]:
         """One pass (eager launches).  Returns, per phantom, rf (n_samples, E, n_tx) and

@@ -108,15 +108,28 @@ def simus_gb300(scatterers, rc, params: TransducerParams, plan: SimusPlan, mediu
                          _native.FSG_OUT_SELECTED_RAW, device)
 
 
-def irfft_and_threshold(full_spectrum: torch.Tensor, plan: SimusPlan) -> torch.Tensor:
-    """rf = irfft(conj(S), n_fft, axis 0)[:(n_fft+1)//2] times the smooth -100 dB gate
-    (simus.py:336-367); cuFFT through torch.fft."""
-    rf = torch.fft.irfft(torch.conj(full_spectrum), n=plan.n_fft, dim=0)
-    rf = rf[: (plan.n_fft + 1) // 2]
-    th = 1e-5
-    mag = rf.abs()
-    rel = mag / (mag.max() + 1e-30)
-    return rf * (0.5 * (1.0 + torch.tanh((rel - th) / (th / 10.0))))
+def irfft_and_threshold(full_spectrum: torch.Tensor, plan: SimusPlan, *, k_first: int = 0, k_count: int | None = None,
+                        gate: bool = True) -> torch.Tensor:
+    """rf = irfft(conj(S), n_fft, axis 0)[:(n_fft+1)//2] times the smooth -100 dB gate with each
+    frame's own peak (simus.py:336-367), by ``fsg_irfft_gate``.  ``full_spectrum`` is one frame
+    (n_freq_full, E) or a batch (B, n_freq_full, E) of complex64 on the GPU; only rows
+    [k_first, k_first + k_count) are read, the others must be zero."""
+    spec = full_spectrum if full_spectrum.dtype == torch.complex64 else full_spectrum.to(torch.complex64)
+    spec = spec.contiguous()
+    batched = spec.dim() == 3
+    frames = spec if batched else spec.unsqueeze(0)
+    nb, n_full, E = frames.shape
+    if k_count is None:
+        k_count = n_full - k_first
+    n_fft = int(plan.n_fft)
+    device = spec.device
+    lib = _native.load()
+    rf = torch.empty((nb, (n_fft + 1) // 2, E), dtype=torch.float32, device=device)
+    ws = _device.workspace(lib.fsg_rf_workspace_size(n_fft, nb), device)
+    _native.check(lib.fsg_irfft_gate(spec.data_ptr(), nb, n_full * E, n_full, E, n_fft, int(k_first), int(k_count),
+                                     1 if gate else 0, rf.data_ptr(), ws.data_ptr(), ws.numel(),
+                                     _device.stream_handle(device)))
+    return rf if batched else rf[0]
 
 
 def simus_compute(scatterers, rc, delays, plan: SimusPlan, params: TransducerParams,
@@ -130,7 +143,8 @@ def simus_compute(scatterers, rc, delays, plan: SimusPlan, params: TransducerPar
     d, a = _delays_apod(delays, tx_apodization, params.n_elements, device)
     full = _launch_simus(scat, r, d, a, plan, params, medium, full_frequency_directivity,
                          _native.FSG_OUT_FULL_CORRECTED, device)
-    return SimusResult(rf=irfft_and_threshold(full, plan), spectrum=full)
+    rf = irfft_and_threshold(full, plan, k_first=int(plan.freq_idx_start), k_count=int(plan.selected_freqs.shape[0]))
+    return SimusResult(rf=rf, spectrum=full)
 
 
 def simus(scatterers, rc, delays, params: TransducerParams, medium: MediumParams = _DEFAULT_MEDIUM, *,

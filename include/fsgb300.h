@@ -255,6 +255,21 @@ int32_t fsg_simus_noalloc(const FsgProbe* probe, const FsgMedium* medium, const 
 /* Size in bytes of fsg_simus_noalloc's static scratch (no counterpart in the reference). */
 size_t fsg_simus_noalloc_scratch_bytes(void);
 
+/*
+ * Spectrum -> RF epilogue.  Replaces _irfft_and_threshold (simus.py:336-367):
+ *   rf = irfft(conj(spectrum), n_fft, axis 0)[: (n_fft + 1) / 2]
+ *   rf *= 0.5 (1 + tanh((|rf| / max|rf| - 1e-5) / 1e-6))        (when gate != 0)
+ * for n_batch frames, each gated with its own peak.  spectrum: n_batch frames of
+ * (n_freq_full, n_elements) complex64, frame b at spectrum + b * batch_stride complex
+ * elements; only rows [k_first, k_first + k_count) are read (the rest must be zero, as in the
+ * zero-padded simus spectrum).  rf_out: (n_batch, (n_fft + 1) / 2, n_elements) float32.
+ * workspace: fsg_rf_workspace_size(n_fft, n_batch) bytes.
+ */
+size_t fsg_rf_workspace_size(int32_t n_fft, int32_t n_batch);
+int32_t fsg_irfft_gate(const void* spectrum, int32_t n_batch, int64_t batch_stride, int32_t n_freq_full,
+                       int32_t n_elements, int32_t n_fft, int32_t k_first, int32_t k_count, int32_t gate,
+                       float* rf_out, void* workspace, size_t workspace_bytes, void* stream);
+
 /* Measurement utility, no counterpart in the reference: launches `blocks` x 256 threads of
  * independent FP32 FMA chains (`iters` iterations) and reports the FLOPs it performs, so a
  * caller can time it with events and state the device's FP32 FMA roofline.  `out` must hold
