@@ -77,7 +77,18 @@ int validate_common(const FsgProbe* probe, const FsgMedium* medium, const FsgFre
   if (probe->n_elements * probe->n_sub > 32 * kSrcPerThread)
     return set_error(FSG_EUNSUPPORTED, "n_elements * n_sub = %d > %d is not supported by this build",
                      probe->n_elements * probe->n_sub, 32 * kSrcPerThread);
-  if (ffd) return set_error(FSG_EUNSUPPORTED, "full_frequency_directivity is not implemented by this build");
+  if (ffd) {
+    // the per-frequency directivity is evaluated as a polynomial valid for |k_f seg / 2| <= 2 pi,
+    // i.e. sub-elements up to two wavelengths of the highest selected frequency wide (the
+    // automatic sub-element count keeps them within about one)
+    const double f_max = plan->freq_start + (plan->n_freq - 1) * plan->freq_step;
+    const double x_max = 2.0 * kPi * f_max / medium->speed_of_sound * plan->seg_length / 2.0;
+    if (x_max > 2.0 * kPi)
+      return set_error(FSG_EUNSUPPORTED,
+                       "full_frequency_directivity with sub-elements wider than two wavelengths "
+                       "(k_max seg / 2 = %.3f > 2 pi) is not supported by this build",
+                       x_max);
+  }
   return FSG_OK;
 }
 
@@ -94,6 +105,7 @@ SweepConst make_sweep_const(const FsgProbe* p, const FsgMedium* m, const FsgFreq
   C.baffle_val = (float)p->baffle_impedance;
   C.baffle = p->baffle;
   C.ffd = ffd;
+  C.half_seg = (float)(plan->seg_length / 2.0);
   return C;
 }
 
@@ -207,7 +219,7 @@ constexpr size_t kGeoCacheBudget = size_t(48) << 20;
 // split into n_slices contiguous slices of per_slice scatterers, one CTA row per slice.
 // cache_budget bounds the geometry cache (chunk_tiles * geo_bytes) from above; a chunk holds
 // at least one tile per slice.
-SweepConfig simus_config(int E, int U, int F, int64_t n_scat, int num_sms, size_t cache_budget) {
+SweepConfig simus_config(int E, int U, int F, int64_t n_scat, int num_sms, size_t cache_budget, int ffd) {
   SweepConfig c;
   const int n_src = E * U;
   c.gn = next_pow2((n_src + kSrcPerThread - 1) / kSrcPerThread);
@@ -218,7 +230,7 @@ SweepConfig simus_config(int E, int U, int F, int64_t n_scat, int num_sms, size_
   c.fb = kAnchor * runs;
   c.n_bands = (F + c.fb - 1) / c.fb;
   c.plane_pad = choose_plane_pad(E, U, c.gn, c.st);
-  const SmemLayout L = smem_layout(c.st, c.fb, E, U, c.plane_pad, true);
+  const SmemLayout L = smem_layout(c.st, c.fb, E, U, c.plane_pad, true, ffd != 0);
   c.smem = L.total;
   c.geo_bytes = L.geo_bytes;
   const int64_t tiles = n_scat > 0 ? (n_scat + c.st - 1) / c.st : 1;
@@ -236,7 +248,7 @@ SweepConfig simus_config(int E, int U, int F, int64_t n_scat, int num_sms, size_
   return c;
 }
 
-SweepConfig pfield_config(int E, int U, int F, int64_t n_pts, int num_sms) {
+SweepConfig pfield_config(int E, int U, int F, int64_t n_pts, int num_sms, int ffd) {
   SweepConfig c;
   const int n_src = E * U;
   c.gn = next_pow2((n_src + kSrcPerThread - 1) / kSrcPerThread);
@@ -254,7 +266,7 @@ SweepConfig pfield_config(int E, int U, int F, int64_t n_pts, int num_sms) {
   c.per_slice = tps * c.st;
   c.n_slices = (int)((tiles + tps - 1) / tps);
   c.plane_pad = choose_plane_pad(E, U, c.gn, c.st);
-  c.smem = smem_layout(c.st, c.fb, E, U, c.plane_pad, false).total;
+  c.smem = smem_layout(c.st, c.fb, E, U, c.plane_pad, false, ffd != 0).total;
   return c;
 }
 
@@ -272,9 +284,16 @@ static size_t simus_ws_size(const SweepConfig& c, int E, int U, int F) {
          align256((size_t)c.chunk_tiles * c.geo_bytes);
 }
 
+// The default workspace, large enough with or without full-frequency directivity (whose
+// geometry block carries one more array).
 static size_t simus_ws_size(const FsgProbe* probe, const FsgFreqPlan* plan, int64_t n_scat, int num_sms) {
-  SweepConfig c = simus_config(probe->n_elements, probe->n_sub, plan->n_freq, n_scat, num_sms, kGeoCacheBudget);
-  return simus_ws_size(c, probe->n_elements, probe->n_sub, plan->n_freq);
+  size_t need = 0;
+  for (int ffd = 0; ffd < 2; ++ffd) {
+    SweepConfig c = simus_config(probe->n_elements, probe->n_sub, plan->n_freq, n_scat, num_sms, kGeoCacheBudget, ffd);
+    const size_t n = simus_ws_size(c, probe->n_elements, probe->n_sub, plan->n_freq);
+    if (n > need) need = n;
+  }
+  return need;
 }
 
 extern "C" size_t fsg_simus_workspace_size(const FsgProbe* probe, const FsgFreqPlan* plan, int64_t n_scat) {
@@ -305,10 +324,10 @@ extern "C" int32_t fsg_simus(const FsgProbe* probe, const FsgMedium* medium, con
   if ((st = device_sm_count(&sms)) != FSG_OK) return st;
   const int E = probe->n_elements, U = probe->n_sub, F = plan->n_freq;
   // the default chunking, or smaller chunks when the caller's workspace is smaller
-  SweepConfig c = simus_config(E, U, F, n_scat, sms, kGeoCacheBudget);
+  SweepConfig c = simus_config(E, U, F, n_scat, sms, kGeoCacheBudget, ffd);
   if (workspace && workspace_bytes < simus_ws_size(c, E, U, F)) {
     const size_t fixed = simus_ws_size(c, E, U, F) - align256((size_t)c.chunk_tiles * c.geo_bytes);
-    if (workspace_bytes > fixed) c = simus_config(E, U, F, n_scat, sms, workspace_bytes - fixed - 256);
+    if (workspace_bytes > fixed) c = simus_config(E, U, F, n_scat, sms, workspace_bytes - fixed - 256, ffd);
   }
   const size_t need = simus_ws_size(c, E, U, F);
   if (!workspace || workspace_bytes < need)
@@ -368,7 +387,7 @@ extern "C" int32_t fsg_simus(const FsgProbe* probe, const FsgMedium* medium, con
 }
 
 static size_t pfield_ws_size(const FsgProbe* probe, const FsgFreqPlan* plan, int64_t n_pts, int num_sms) {
-  SweepConfig c = pfield_config(probe->n_elements, probe->n_sub, plan->n_freq, n_pts, num_sms);
+  SweepConfig c = pfield_config(probe->n_elements, probe->n_sub, plan->n_freq, n_pts, num_sms, 0);
   return tables_bytes(probe->n_elements, probe->n_sub, plan->n_freq) + align256((size_t)c.n_bands * n_pts * 4);
 }
 
@@ -398,7 +417,7 @@ extern "C" int32_t fsg_pfield(const FsgProbe* probe, const FsgMedium* medium, co
   Tables t = carve_tables(ws, E, U, F);
   float* partial = reinterpret_cast<float*>(ws + tables_bytes(E, U, F));
   if ((st = launch_setup(probe, medium, plan, delays, apod, t, s)) != FSG_OK) return st;
-  SweepConfig c = pfield_config(E, U, F, n_points, sms);
+  SweepConfig c = pfield_config(E, U, F, n_points, sms, ffd);
   BandArgs A;
   A.pts = points;
   A.rc = nullptr;

@@ -136,7 +136,48 @@ struct SweepConst {
   float baffle_val; // impedance ratio for FSG_BAFFLE_IMPEDANCE
   int baffle;       // 0 soft, 1 rigid, 2 impedance
   int ffd;          // full-frequency directivity (directivity applied per frequency)
+  float half_seg;   // seg_length / 2: the per-frequency directivity argument is k_f * half_seg * sin(theta)
 };
+
+// sin(x)/x for |x| <= 2 pi as its Taylor series to x^26 in u = x^2 (truncation < 3e-9 there;
+// FP32 rounding adds at most ~3e-6 absolute at the end of the range, where the terms are
+// largest): the per-frequency directivity of full_frequency_directivity
+// (_simus_strategies.py:59-62, _pfield_strategies.py:77-81).
+constexpr int kSincTerms = 14;
+__device__ __forceinline__ float sinc_coef(int n) {  // (-1)^n / (2n + 1)!
+  constexpr float c[kSincTerms] = {1.0f,
+                                   -1.0f / 6.0f,
+                                   1.0f / 120.0f,
+                                   -1.0f / 5040.0f,
+                                   1.0f / 362880.0f,
+                                   -1.0f / 39916800.0f,
+                                   1.0f / 6227020800.0f,
+                                   -1.0f / 1307674368000.0f,
+                                   1.0f / 355687428096000.0f,
+                                   -1.0f / 121645100408832000.0f,
+                                   1.0f / 51090942171709440000.0f,
+                                   -1.0f / 25852016738884976640000.0f,
+                                   1.0f / 15511210043330985984000000.0f,
+                                   -1.0f / 10888869450418352160768000000.0f};
+  return c[n];
+}
+
+__device__ __forceinline__ float sinc_poly(float x) {
+  const float u = x * x;
+  float p = sinc_coef(kSincTerms - 1);
+#pragma unroll
+  for (int n = kSincTerms - 2; n >= 0; --n) p = fmaf(p, u, sinc_coef(n));
+  return p;
+}
+
+// sinc_poly of both lanes on the packed FP32x2 pipe.
+__device__ __forceinline__ float2 sinc_poly2(float2 x) {
+  const float2 u = __fmul2_rn(x, x);
+  float2 p = make_float2(sinc_coef(kSincTerms - 1), sinc_coef(kSincTerms - 1));
+#pragma unroll
+  for (int n = kSincTerms - 2; n >= 0; --n) p = __ffma2_rn(p, u, make_float2(sinc_coef(n), sinc_coef(n)));
+  return p;
+}
 
 // sin(x)/x: Taylor series for |x| < 2 (truncation error < 3e-9), sinf(x)/x beyond.
 __device__ __forceinline__ float sinc_rad(float x) {
@@ -163,6 +204,7 @@ __device__ __forceinline__ float sinc_rad(float x) {
 struct SrcGeo {
   float r_hi, r_lo, amp;
   float2 step;
+  float sth;  // sin(theta)
 };
 
 __device__ __forceinline__ SrcGeo source_geometry(dfl xs, dfl zs, float4 sp, float2 rot, const SweepConst& C) {
@@ -186,6 +228,7 @@ __device__ __forceinline__ SrcGeo source_geometry(dfl xs, dfl zs, float4 sp, flo
   const float mag = (C.dalpha != 0.0f) ? expf(-C.dalpha * r.hi) : 1.0f;
   const float2 cis = df_cis_accurate(C.dk, r.hi, r.lo);
   g.step = make_float2(mag * cis.x, mag * cis.y);
+  g.sth = sth;
   return g;
 }
 

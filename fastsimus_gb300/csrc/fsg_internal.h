@@ -59,13 +59,15 @@ struct SmemLayout {
   // (consecutive elements) conflict-free; plane_pad spreads the transmit accesses (lanes =
   // sources g + GN i of one or more points) over the banks.
   int pitch, plane;
-  size_t off_rhi, off_rlo, off_amp, off_step, off_w, off_pp, off_ka, off_aa, off_da, off_y, total;
-  size_t geo_bytes;    // the four geometry arrays, contiguous from offset 0
+  size_t off_rhi, off_rlo, off_amp, off_step, off_dir, off_w, off_pp, off_kb, off_ka, off_aa, off_da, off_y, total;
+  size_t geo_bytes;    // the geometry arrays, contiguous from offset 0
 };
 
 __host__ __device__ inline size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
 
-__host__ __device__ inline SmemLayout smem_layout(int st, int fb, int E, int U, int plane_pad, bool with_w) {
+// With ffd, a fifth geometry array holds half_seg * sin(theta) per (source, point).
+__host__ __device__ inline SmemLayout smem_layout(int st, int fb, int E, int U, int plane_pad, bool with_w,
+                                                  bool ffd = false) {
   SmemLayout L;
   L.pitch = st + 1;
   L.plane = E * L.pitch + plane_pad;
@@ -75,9 +77,11 @@ __host__ __device__ inline SmemLayout smem_layout(int st, int fb, int E, int U, 
   L.off_rlo = o; o = align16(o + n * 4);
   L.off_amp = o; o = align16(o + n * 4);
   L.off_step = o; o = align16(o + n * 8);
+  L.off_dir = o; o = align16(o + (ffd ? n * 4 : 0));
   L.geo_bytes = o;
   L.off_w = o; o = align16(o + (with_w ? (size_t)fb * st * 8 : 0));
   L.off_pp = o; o = align16(o + (size_t)fb * 8);
+  L.off_kb = o; o = align16(o + (size_t)fb * 4);  // FP32 wavenumber of each band frequency
   int na = fb / kAnchor;
   L.off_ka = o; o = align16(o + (size_t)na * 8);
   L.off_aa = o; o = align16(o + (size_t)na * 4);

@@ -1,22 +1,20 @@
-// Plain fused FP32 simus and pfield sweeps for GB300 (sm_103a).
+// Plain fused FP32 simus and pfield sweeps for GB300 (sm_103a): set-up tables, the geometry
+// pre-pass, the reductions and the launch dispatch.  The band kernels themselves are templates
+// in fsg_sweep_kernels.cuh.
 //
-// Work decomposition (one CTA = 256 threads):
-//   blockIdx.x -> a frequency band of `fb` consecutive selected frequencies
-//   blockIdx.y -> a slice of scatterers (simus) or grid points (pfield)
-// A CTA walks its slice in tiles of `st` scatterers.  For each tile:
-//   1. geometry: each thread computes the double-float distance, amplitude and recurrence
-//      step of kSrcPerThread (scatterer, source) pairs and parks them in shared memory;
-//   2. TX: the same thread advances its 16 transmit-weighted Green's terms through the band
-//      (re-anchored every kAnchor steps), sums them, and the `gn` threads that share a
-//      scatterer finish the sum over all E*U sources with warp shuffles.  The product
-//      rc * pulse * probe * P is the scattered field W[s][f] (simus) or |.|^2 is
-//      accumulated per point (pfield);
-//   3. RX (simus): thread (element e, run of kAnchor frequencies) re-generates the receive
-//      Green's terms of every scatterer of the tile from the parked geometry and accumulates
-//      Y[e][f] += W[s][f] * mean_u G(s, e, u, f) in registers (per tile; the running sum
-//      over tiles sits in shared memory).
-// Neither the scatterer x element Green's tile nor W ever leaves the SM; the only global
-// output is one (F x E) partial spectrum per slice, summed in a fixed order by fsg_reduce.
+// simus, per chunk of scatterers:
+//   geometry_kernel    once per (scatterer, source): double-float distance, amplitude
+//                      (obliquity x centre-frequency sinc / sqrt(r) / n_sub), recurrence step
+//                      (and half_seg sin(theta) with full-frequency directivity), written as
+//                      one shared-memory-layout block per tile into an L2-sized cache;
+//   simus_band_kernel  grid (frequency band, slice of tiles); per tile: TMA bulk copy of the
+//                      tile's block, TX (packed FP32x2 recurrences, reduce-scatter of the
+//                      source sums across the point's lanes, W[s][f] = rc pulse probe P), RX
+//                      (thread = element x 32 frequencies, Y[e][f] += W[s][f] mean_u G);
+// then simus_reduce sums the slices' partial spectra in a fixed order.  Neither the
+// scatterer x element Green's tile nor W ever leaves the SM.
+// pfield: pfield_band_kernel computes its geometry in place (3 bands share little) and
+// accumulates |pulse probe P|^2; pfield_reduce sums the bands and takes the square root.
 
 #include <cuda_runtime.h>
 #include <math.h>
@@ -24,13 +22,11 @@
 
 #include "fsg_common.cuh"
 #include "fsg_internal.h"
-#include "fsg_tc.cuh"
+#include "fsg_sweep_kernels.cuh"
 
 namespace fsg {
 
 constexpr double kNeperToDb = 8.685889638065035;  // 20 / ln(10)
-constexpr size_t kBulkPiece = 32 * 1024;            // bytes per TMA bulk copy instruction
-constexpr uint32_t kBulkWaitTries = 1u << 26;       // bound on the polls of one copy's mbarrier
 
 // Element / sub-element positions (utils/geometry.py:18-88, _pfield_math.py:40-67),
 // per-frequency wavenumber / attenuation / spectra, per-anchor delay-apodization factors.
@@ -89,44 +85,6 @@ __global__ void setup_tables(SetupArgs a) {
   }
 }
 
-__device__ __forceinline__ dfl load_coord(const double* p) {
-  return split_double(*p);
-}
-
-// Loads the band's per-frequency tables into shared memory.
-__device__ __forceinline__ void load_band_tables(const BandArgs& A, const SmemLayout& L, unsigned char* sm, int f_b0) {
-  float2* pp = reinterpret_cast<float2*>(sm + L.off_pp);
-  float2* ka = reinterpret_cast<float2*>(sm + L.off_ka);
-  float* aa = reinterpret_cast<float*>(sm + L.off_aa);
-  float2* da = reinterpret_cast<float2*>(sm + L.off_da);
-  const int na = A.fb / kAnchor;
-  for (int i = threadIdx.x; i < A.fb; i += blockDim.x) {
-    int f = f_b0 + i;
-    pp[i] = (f < A.F) ? A.t.pp[f] : make_float2(0.f, 0.f);
-  }
-  for (int m = threadIdx.x; m < na; m += blockDim.x) {
-    int f = min(f_b0 + m * kAnchor, A.F - 1);
-    ka[m] = A.t.kf[f];
-    aa[m] = A.t.af[f];
-  }
-  for (int i = threadIdx.x; i < na * A.E; i += blockDim.x) {
-    int m = i / A.E, e = i % A.E;
-    int ga = min(f_b0 / kAnchor + m, A.n_anchor - 1);
-    da[i] = A.t.da[ga * A.E + e];
-  }
-}
-
-// Geometry of one (point, source) into the four geometry arrays at word index idx.
-__device__ __forceinline__ void store_geometry(float* rhi, float* rlo, float* amp, float2* stp, int idx, dfl xs, dfl zs,
-                                               const BandArgs& A, int src) {
-  const int e = src / A.U;
-  const SrcGeo geo = source_geometry(xs, zs, A.t.src_pos[src], A.t.rot_e[e], A.C);
-  rhi[idx] = geo.r_hi;
-  rlo[idx] = geo.r_lo;
-  amp[idx] = geo.amp;
-  stp[idx] = geo.step;
-}
-
 // Geometry of a chunk's tiles, once per (scatterer, source) for all frequency bands.  A CTA
 // takes one tile at a time: its scatterers' coordinates are split into double-float pairs
 // once, then thread i handles (source, point) items i, i + 256, ...; consecutive threads take
@@ -134,7 +92,7 @@ __device__ __forceinline__ void store_geometry(float* rhi, float* rlo, float* am
 // scatterer list repeat the tile's first point (their rc is 0 in the band kernel).
 __global__ void __launch_bounds__(kThreads) geometry_kernel(const BandArgs A, int64_t chunk_tiles) {
   __shared__ float4 xz[kThreads];  // st <= 64 points of the tile
-  const SmemLayout L = smem_layout(A.st, A.fb, A.E, A.U, A.plane_pad, true);
+  const SmemLayout L = smem_layout(A.st, A.fb, A.E, A.U, A.plane_pad, true, A.C.ffd != 0);
   const int items = A.n_src * A.st;
   for (int64_t tile = blockIdx.x; tile < chunk_tiles; tile += gridDim.x) {
     __syncthreads();
@@ -150,296 +108,12 @@ __global__ void __launch_bounds__(kThreads) geometry_kernel(const BandArgs A, in
     float* rlo = reinterpret_cast<float*>(blk + L.off_rlo);
     float* amp = reinterpret_cast<float*>(blk + L.off_amp);
     float2* stp = reinterpret_cast<float2*>(blk + L.off_step);
+    float* dir = A.C.ffd ? reinterpret_cast<float*>(blk + L.off_dir) : nullptr;
     for (int it = threadIdx.x; it < items; it += blockDim.x) {
       const int pt = it % A.st, src = it / A.st;
       const int e = src / A.U, u = src - e * A.U;
       const float4 c = xz[pt];
-      store_geometry(rhi, rlo, amp, stp, u * L.plane + e * L.pitch + pt, dfl{c.x, c.y}, dfl{c.z, c.w}, A, src);
-    }
-  }
-}
-
-// TX over one band for one tile (with the tile's geometry computed here first when kGeo).
-// Each thread owns point `sl` of the tile and sources g + GN i (i < 16); the GN threads of a
-// point are GN adjacent lanes of one warp.  Frequencies are processed in blocks of GN steps:
-// every lane keeps its partial source sums of the block, then a reduce-scatter across the GN
-// lanes (log2 GN shuffle levels, halving the exchanged values each level) leaves lane g with
-// the full sum of frequency block + g.  `sink(f_local, psum)` is therefore called by every
-// lane, once per block, each for its own frequency.
-template <int GN, bool kGeo, class Sink>
-__device__ __forceinline__ void tx_tile(const BandArgs& A, const SmemLayout& L, unsigned char* sm, int64_t p_idx,
-                                        int sl, int g, Sink& sink) {
-  float* b_rhi = reinterpret_cast<float*>(sm + L.off_rhi);
-  float* b_rlo = reinterpret_cast<float*>(sm + L.off_rlo);
-  float* b_amp = reinterpret_cast<float*>(sm + L.off_amp);
-  float2* b_st = reinterpret_cast<float2*>(sm + L.off_step);
-  const float2* ka = reinterpret_cast<const float2*>(sm + L.off_ka);
-  const float* aa = reinterpret_cast<const float*>(sm + L.off_aa);
-  const float2* da = reinterpret_cast<const float2*>(sm + L.off_da);
-
-  // 1. geometry of my sources, parked in shared memory (rolled loop: one copy of the code)
-  if constexpr (kGeo) {
-    const dfl xs = load_coord(A.pts + 2 * p_idx);
-    const dfl zs = load_coord(A.pts + 2 * p_idx + 1);
-#pragma unroll 1
-    for (int i = 0; i < kSrcPerThread; ++i) {
-      const int src = g + GN * i;
-      if (src < A.n_src) {
-        const int e = src / A.U, u = src - e * A.U;
-        store_geometry(b_rhi, b_rlo, b_amp, b_st, u * L.plane + e * L.pitch + sl, xs, zs, A, src);
-      }
-    }
-  }
-  // 2. transmit sweep: exact anchor every kTxAnchor steps, FP32 recurrence in between.
-  // The thread's sources i = 2p and 2p+1 share one packed FP32x2 lane pair (real and
-  // imaginary parts in separate pairs), so a step costs four packed instructions per two
-  // sources and the source sum two packed adds.
-  constexpr int kPairs = kSrcPerThread / 2;
-  float2 Gr[kPairs], Gi[kPairs], Sr[kPairs], Si[kPairs], Sn[kPairs];
-  const int n_tx_anchor = (A.fb + kTxAnchor - 1) / kTxAnchor;
-  for (int m = 0; m < n_tx_anchor; ++m) {
-    const int am = m * (kTxAnchor / kAnchor);  // index into the band's kAnchor-spaced tables
-#pragma unroll
-    for (int p = 0; p < kPairs; ++p) {
-      float2 gv[2], sv[2];
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int src = g + GN * (2 * p + h);
-        gv[h] = make_float2(0.f, 0.f);
-        sv[h] = make_float2(0.f, 0.f);
-        if (src < A.n_src) {
-          const int e = src / A.U, u = src - e * A.U;
-          const int idx = u * L.plane + e * L.pitch + sl;
-          gv[h] = cmul(anchor_value(b_rhi[idx], b_rlo[idx], b_amp[idx], ka[am], aa[am]), da[am * A.E + e]);
-          if (m == 0) sv[h] = cmul(b_st[idx], A.t.dstep[e]);
-        }
-      }
-      Gr[p] = make_float2(gv[0].x, gv[1].x);
-      Gi[p] = make_float2(gv[0].y, gv[1].y);
-      if (m == 0) {
-        Sr[p] = make_float2(sv[0].x, sv[1].x);
-        Si[p] = make_float2(sv[0].y, sv[1].y);
-        Sn[p] = make_float2(-sv[0].y, -sv[1].y);
-      }
-    }
-    const int n_steps = min(kTxAnchor, A.fb - m * kTxAnchor);  // a multiple of kAnchor, so of GN
-#pragma unroll 1
-    for (int jb = 0; jb < n_steps; jb += GN) {
-      float vr[GN], vi[GN];
-#pragma unroll
-      for (int j = 0; j < GN; ++j) {
-        float2 ar = Gr[0], ai = Gi[0];
-        cstep2(Gr[0], Gi[0], Sr[0], Si[0], Sn[0]);
-#pragma unroll
-        for (int p = 1; p < kPairs; ++p) {
-          ar = __fadd2_rn(ar, Gr[p]);
-          ai = __fadd2_rn(ai, Gi[p]);
-          cstep2(Gr[p], Gi[p], Sr[p], Si[p], Sn[p]);
-        }
-        vr[j] = ar.x + ar.y;
-        vi[j] = ai.x + ai.y;
-      }
-      // reduce-scatter: at level h the lane with bit h set keeps the upper half of its values
-#pragma unroll
-      for (int h = GN / 2; h >= 1; h >>= 1) {
-        const bool up = (g & h) != 0;
-#pragma unroll
-        for (int i = 0; i < h; ++i) {
-          const float sr = up ? vr[i] : vr[i + h], si = up ? vi[i] : vi[i + h];
-          const float kr = up ? vr[i + h] : vr[i], ki = up ? vi[i + h] : vi[i];
-          vr[i] = kr + __shfl_xor_sync(0xffffffffu, sr, h);
-          vi[i] = ki + __shfl_xor_sync(0xffffffffu, si, h);
-        }
-      }
-      sink(m * kTxAnchor + jb + g, make_float2(vr[0], vi[0]));
-    }
-  }
-}
-
-struct SimusSink {
-  float2* W;        // [st][fb]
-  const float2* pp; // [fb]
-  float w;          // rc (0 when out of field or padding)
-  int sl, fb;
-  __device__ __forceinline__ void operator()(int fl, float2 ps) {
-    float2 v = cmul(pp[fl], ps);
-    W[sl * fb + fl] = make_float2(w * v.x, w * v.y);
-  }
-};
-
-template <int U, int GN>
-__global__ void __launch_bounds__(kThreads, 1) simus_band_kernel(const BandArgs A) {
-  extern __shared__ __align__(16) unsigned char sm[];
-  const SmemLayout L = smem_layout(A.st, A.fb, A.E, A.U, A.plane_pad, true);
-  __shared__ uint64_t s_mbar;
-  __shared__ int s_fail;
-  const int tid = threadIdx.x;
-  const int f_b0 = blockIdx.x * A.fb;
-  const int64_t s_begin = A.chunk_s0 + (int64_t)blockIdx.y * A.per_slice;
-  const int64_t s_end = min(A.n_pts, s_begin + A.per_slice);
-  load_band_tables(A, L, sm, f_b0);
-  if (tid == 0) {
-    tc::mbar_init(&s_mbar, 1);
-    tc::fence_mbar_init();
-    s_fail = 0;
-  }
-
-  const int g = tid % GN;
-  const int sl = tid / GN;  // < st by construction (gn * st == 256)
-  const int n_runs = A.fb / kAnchor;
-  const bool rx_on = tid < A.E * n_runs;
-  const int e_rx = tid % A.E;
-  const int run = tid / A.E;
-
-  // Running receive spectrum of this thread, kept in shared memory ([j][thread]) so the
-  // registers go to the per-tile partials and the recurrence state.
-  float2* Ys = reinterpret_cast<float2*>(sm + L.off_y);
-#pragma unroll
-  for (int j = 0; j < kAnchor; ++j) Ys[j * kThreads + tid] = make_float2(0.f, 0.f);
-
-  float* b_rhi = reinterpret_cast<float*>(sm + L.off_rhi);
-  float* b_rlo = reinterpret_cast<float*>(sm + L.off_rlo);
-  float* b_amp = reinterpret_cast<float*>(sm + L.off_amp);
-  float2* b_st = reinterpret_cast<float2*>(sm + L.off_step);
-  float2* W = reinterpret_cast<float2*>(sm + L.off_w);
-  const float2* pp = reinterpret_cast<const float2*>(sm + L.off_pp);
-  __syncthreads();
-
-  const float2 k_run = A.t.kf[min(f_b0 + (rx_on ? run : 0) * kAnchor, A.F - 1)];
-  const float a_run = A.t.af[min(f_b0 + (rx_on ? run : 0) * kAnchor, A.F - 1)];
-
-  uint32_t phase = 0;
-  for (int64_t t0 = s_begin; t0 < s_end; t0 += A.st) {
-    // ---------------- geometry: TMA bulk copy of the tile's block ----------------
-    // The previous tile's reads of these arrays finished at the barrier that closed it; the
-    // proxy fence orders them before the asynchronous writes.  Thread 0 waits (bounded) and
-    // the barrier publishes the data and the outcome to the CTA.
-    if (tid == 0) {
-      const unsigned char* src = A.geo + ((t0 - A.chunk_s0) / A.st) * A.geo_bytes;
-      tc::fence_proxy_async_smem();
-      tc::mbar_arrive_expect_tx(&s_mbar, (uint32_t)A.geo_bytes);
-      for (size_t off = 0; off < A.geo_bytes; off += kBulkPiece)
-        tc::bulk_g2s(sm + off, src + off, (uint32_t)min(kBulkPiece, A.geo_bytes - off), &s_mbar);
-      if (!tc::mbar_wait_bounded(&s_mbar, phase, kBulkWaitTries)) s_fail = 1;
-    }
-    phase ^= 1u;
-    __syncthreads();
-    if (s_fail) break;
-    // ---------------- TX ----------------
-    {
-      int64_t s = t0 + sl;
-      bool valid = s < s_end;
-      int64_t si = valid ? s : t0;
-      float w = 0.f;
-      if (valid) {
-        double x = A.pts[2 * si], z = A.pts[2 * si + 1];
-        bool out = z < 0.0;
-        if (A.convex) out = out || (x * x + (z + A.apex) * (z + A.apex) <= A.radius2);
-        w = out ? 0.f : (float)A.rc[si];
-      }
-      SimusSink sink{W, pp, w, sl, A.fb};
-      tx_tile<GN, false>(A, L, sm, si, sl, g, sink);
-    }
-    __syncthreads();
-    // ---------------- RX ----------------
-    if (rx_on) {
-      float2 Yt[kAnchor];
-#pragma unroll
-      for (int j = 0; j < kAnchor; ++j) Yt[j] = make_float2(0.f, 0.f);
-#pragma unroll 1
-      // two scatterers per pass (st is even): independent recurrences give the scheduler two
-      // chains per sub-element to interleave; both accumulate into the same partial
-      for (int s = 0; s < A.st; s += 2) {
-        // the scatterers' fields over my run of frequencies: contiguous, read 2 per load
-        const float4* Wa = reinterpret_cast<const float4*>(W + s * A.fb + run * kAnchor);
-        const float4* Wb = reinterpret_cast<const float4*>(W + (s + 1) * A.fb + run * kAnchor);
-        float2 Ga[U], Sa[U], Gb[U], Sb[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int idx = u * L.plane + e_rx * L.pitch + s;
-          Ga[u] = anchor_value(b_rhi[idx], b_rlo[idx], b_amp[idx], k_run, a_run);
-          Sa[u] = b_st[idx];
-          Gb[u] = anchor_value(b_rhi[idx + 1], b_rlo[idx + 1], b_amp[idx + 1], k_run, a_run);
-          Sb[u] = b_st[idx + 1];
-        }
-#pragma unroll
-        for (int j = 0; j < kAnchor; ++j) {
-          float2 ra = Ga[0], rb = Gb[0];
-          Ga[0] = cmul(Ga[0], Sa[0]);
-          Gb[0] = cmul(Gb[0], Sb[0]);
-#pragma unroll
-          for (int u = 1; u < U; ++u) {
-            ra = cadd(ra, Ga[u]);
-            rb = cadd(rb, Gb[u]);
-            Ga[u] = cmul(Ga[u], Sa[u]);
-            Gb[u] = cmul(Gb[u], Sb[u]);
-          }
-          const float4 wa = Wa[j >> 1], wb = Wb[j >> 1];
-          Yt[j] = cfma((j & 1) ? make_float2(wa.z, wa.w) : make_float2(wa.x, wa.y), ra, Yt[j]);
-          Yt[j] = cfma((j & 1) ? make_float2(wb.z, wb.w) : make_float2(wb.x, wb.y), rb, Yt[j]);
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < kAnchor; ++j) Ys[j * kThreads + tid] = cadd(Ys[j * kThreads + tid], Yt[j]);
-    }
-    __syncthreads();
-  }
-  if (s_fail && tid == 0) atomicExch(A.status, FSG_ETIMEOUT);
-  if (rx_on) {
-    float2* out = reinterpret_cast<float2*>(A.partial) + (size_t)blockIdx.y * A.F * A.E;
-#pragma unroll
-    for (int j = 0; j < kAnchor; ++j) {
-      int f = f_b0 + run * kAnchor + j;
-      if (f < A.F) {
-        const float2 y = Ys[j * kThreads + tid];
-        float2* o = out + (size_t)f * A.E + e_rx;
-        *o = A.accumulate ? cadd(*o, y) : y;
-      }
-    }
-  }
-}
-
-struct PfieldSink {
-  const float2* pp;
-  float acc;
-  int fb_valid;
-  __device__ __forceinline__ void operator()(int fl, float2 ps) {
-    if (fl < fb_valid) {
-      float2 v = cmul(pp[fl], ps);
-      acc = fmaf(v.x, v.x, fmaf(v.y, v.y, acc));
-    }
-  }
-};
-
-template <int GN>
-__global__ void __launch_bounds__(kThreads, GN >= 32 ? 1 : 2) pfield_band_kernel(const BandArgs A) {
-  extern __shared__ __align__(16) unsigned char sm[];
-  const SmemLayout L = smem_layout(A.st, A.fb, A.E, A.U, A.plane_pad, false);
-  const int tid = threadIdx.x;
-  const int f_b0 = blockIdx.x * A.fb;
-  const int64_t p_begin = (int64_t)blockIdx.y * A.per_slice;
-  const int64_t p_end = min(A.n_pts, p_begin + A.per_slice);
-  load_band_tables(A, L, sm, f_b0);
-  __syncthreads();
-  const int g = tid % GN;
-  const int sl = tid / GN;
-  const float2* pp = reinterpret_cast<const float2*>(sm + L.off_pp);
-  float* out = reinterpret_cast<float*>(A.partial) + (size_t)blockIdx.x * A.n_pts;
-  for (int64_t t0 = p_begin; t0 < p_end; t0 += A.st) {
-    int64_t p = t0 + sl;
-    bool valid = p < p_end;
-    int64_t pi = valid ? p : t0;
-    PfieldSink sink{pp, 0.f, min(A.fb, A.F - f_b0)};
-    tx_tile<GN, true>(A, L, sm, pi, sl, g, sink);
-    // each lane holds the band's |p|^2 over its own frequencies: sum the GN lanes in a fixed tree
-    float acc = sink.acc;
-#pragma unroll
-    for (int off = 1; off < GN; off <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-    if (valid && g == 0) {
-      double x = A.pts[2 * pi], z = A.pts[2 * pi + 1];
-      bool o = z < 0.0;
-      if (A.convex) o = o || (x * x + (z + A.apex) * (z + A.apex) <= A.radius2);
-      out[pi] = o ? 0.f : acc;
+      store_geometry(rhi, rlo, amp, stp, dir, u * L.plane + e * L.pitch + pt, dfl{c.x, c.y}, dfl{c.z, c.w}, A, src);
     }
   }
 }
@@ -474,52 +148,12 @@ __global__ void pfield_reduce(const float* __restrict__ partial, int n_bands, in
   out[i] = sqrtf(acc * corr);
 }
 
-template <int U, int GN>
-static cudaError_t launch_simus_band(const SweepConfig& c, const BandArgs& A, cudaStream_t s) {
-  cudaError_t e =
-      cudaFuncSetAttribute(simus_band_kernel<U, GN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem);
-  if (e != cudaSuccess) return e;
-  simus_band_kernel<U, GN><<<dim3(c.n_bands, c.n_slices), kThreads, c.smem, s>>>(A);
-  return cudaGetLastError();
-}
-
-template <int U>
-static cudaError_t launch_simus_band_gn(const SweepConfig& c, const BandArgs& A, cudaStream_t s) {
-  switch (c.gn) {
-    case 4: return launch_simus_band<U, 4>(c, A, s);
-    case 8: return launch_simus_band<U, 8>(c, A, s);
-    case 16: return launch_simus_band<U, 16>(c, A, s);
-    case 32: return launch_simus_band<U, 32>(c, A, s);
-    default: return cudaErrorInvalidValue;
-  }
-}
-
 cudaError_t launch_simus_band_any(int U, const SweepConfig& c, const BandArgs& A, cudaStream_t s) {
-  switch (U) {
-    case 1: return launch_simus_band_gn<1>(c, A, s);
-    case 2: return launch_simus_band_gn<2>(c, A, s);
-    case 3: return launch_simus_band_gn<3>(c, A, s);
-    case 4: return launch_simus_band_gn<4>(c, A, s);
-    default: return cudaErrorInvalidValue;
-  }
-}
-
-template <int GN>
-static cudaError_t launch_pfield_band(const SweepConfig& c, const BandArgs& A, cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(pfield_band_kernel<GN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem);
-  if (e != cudaSuccess) return e;
-  pfield_band_kernel<GN><<<dim3(c.n_bands, c.n_slices), kThreads, c.smem, s>>>(A);
-  return cudaGetLastError();
+  return A.C.ffd ? launch_simus_band_ffd(U, c, A, s) : launch_simus_band_u<false>(U, c, A, s);
 }
 
 cudaError_t launch_pfield_band_any(const SweepConfig& c, const BandArgs& A, cudaStream_t s) {
-  switch (c.gn) {
-    case 4: return launch_pfield_band<4>(c, A, s);
-    case 8: return launch_pfield_band<8>(c, A, s);
-    case 16: return launch_pfield_band<16>(c, A, s);
-    case 32: return launch_pfield_band<32>(c, A, s);
-    default: return cudaErrorInvalidValue;
-  }
+  return A.C.ffd ? launch_pfield_band_ffd(c, A, s) : launch_pfield_band_gn<false>(c, A, s);
 }
 
 }  // namespace fsg

@@ -9,7 +9,7 @@ from tests._gpu import np64, require_gpu
 
 pytestmark = pytest.mark.gpu
 
-CASES = [n for n in G.names("pfield_") if "ffd" not in n]
+CASES = G.names("pfield_")
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -22,7 +22,8 @@ def test_pfield_matches_reference_golden(name):
     import fastsimus_gb300 as F
 
     g = G.load(name)
-    out = np64(F.pfield(g.positions, g.delays, g.params, g.medium, tx_apodization=g.apod))
+    out = np64(F.pfield(g.positions, g.delays, g.params, g.medium, tx_apodization=g.apod,
+                        full_frequency_directivity=g.ffd))
     assert out.shape == g.prms.shape
     err = G.rel_l2(out, g.prms)
     print(f"{name}: relL2 = {err:.3e}")

@@ -12,7 +12,7 @@ from tests._gpu import np64, require_gpu, torch
 pytestmark = pytest.mark.gpu
 
 PLAIN_TOL = 1e-5
-CASES = [n for n in G.names("simus_") if not n.startswith("simus_multi") and "ffd" not in n]
+CASES = [n for n in G.names("simus_") if not n.startswith("simus_multi")]
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -26,7 +26,7 @@ def test_simus_rf_matches_reference_golden(name):
 
     g = G.load(name)
     res = F.simus(g.scatterers, g.rc, g.delays, g.params, g.medium, fs=g.fs, tx_apodization=g.apod,
-                  element_splitting=g.element_splitting)
+                  element_splitting=g.element_splitting, full_frequency_directivity=g.ffd)
     rf = np64(res.rf)
     assert rf.shape == g.rf.shape
     err = G.rel_l2(rf, g.rf)
@@ -122,12 +122,19 @@ def test_deterministic_bitwise():
     assert torch.equal(x, y)
 
 
-def test_ffd_unsupported_raises():
+def test_ffd_wide_subelements_raise():
+    """Full-frequency directivity is supported while k_max seg/2 <= pi (the automatic
+    sub-element rule); forcing one sub-element across a multi-wavelength element is refused
+    instead of silently losing accuracy."""
     import fastsimus_gb300 as F
+    from fastsimus_gb300.params import TransducerParams
 
     g = G.load("simus_small_ffd")
+    p = g.params
+    wide = TransducerParams(freq_center=p.freq_center, pitch=4 * p.pitch, n_elements=p.n_elements,
+                            width=3.5 * p.pitch, bandwidth=p.bandwidth, baffle=p.baffle)
     with pytest.raises(NotImplementedError):
-        F.simus(g.scatterers, g.rc, g.delays, g.params, g.medium, full_frequency_directivity=True)
+        F.simus(g.scatterers, g.rc, g.delays, wide, g.medium, full_frequency_directivity=True, element_splitting=1)
 
 
 def test_cpu_strategies_raise():
