@@ -42,7 +42,7 @@ class BatchTuning:
 
     @staticmethod
     def default(backend: str) -> "BatchTuning":
-        return BatchTuning(7, 65536, 1) if backend == "tc" else BatchTuning()
+        return BatchTuning(7, 16384, 1) if backend == "tc" else BatchTuning()
 
     def to_c(self) -> _native.FsgBatchTuning:
         return _native.FsgBatchTuning(self.freqs_per_item, self.chunk_scatterers, self.ctas_per_sm, 0)
@@ -207,7 +207,7 @@ class BatchedSimus:
             self.set_tuning(best)
             return best
         if candidates is None and self.backend == "tc":
-            candidates = [BatchTuning(fb, 65536, 1) for fb in (4, 5, 6, 7)]
+            candidates = [BatchTuning(fb, c, 1) for fb in (5, 6, 7) for c in (8192, 16384)]
         if candidates is None:
             total = sum(int(s.shape[0]) for s, _ in self.phantoms)
             chunks = sorted({c for c in (8192, 16384, 32768, 65536, 131072) if c < 2 * max(total, 64)} or {8192})

@@ -16,6 +16,7 @@ struct BatchPhantom {
   const double* scat;       // [n_scat*2]
   const double* rc;         // [n_scat]
   int64_t n_scat;
+  int64_t tile0;            // tensor-core path: this phantom's first tile in the geometry cache
   int n_freq, n_freq_full, freq_idx_start, n_bands, n_chunks, item0;
   double f0, df;
   float corr;

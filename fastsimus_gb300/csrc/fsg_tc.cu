@@ -51,16 +51,15 @@ struct TcArgs {
   int* queue;
   int* status;
   float2* partial;  // [n_items][fb][kTcTx][kTcE]
+  const float4* geo;  // per (tile, state, thread) geometry of all phantoms, see tc_geometry_kernel
 };
 
 // Geometry for the tensor-core path (accuracy target 1e-3), in plain FP32 and without
-// branches so that a thread's eight staged states overlap: distance from one rsqrt, anchor
-// phase k0 r reduced mod 2 pi in FP32 (error ~1e-7 |k0 r|, below 1e-4 rad here), MUFU
-// sin/cos/exp for the anchor and for the recurrence step (whose ~4e-7 error compounds over at
-// most six steps).  Obliquity, the 1e-16 horizon floor, the centre-frequency sinc and the
-// lambda/2 clip follow _pfield_math.py:70-118 and :165-199 as in the plain kernels.
-__device__ __forceinline__ void tc_source(float xs, float zs, float4 sp, float2 rot, const SweepConst& C, float2 k0,
-                                          float a0, float2& g, float2& st) {
+// branches: distance from one rsqrt, the lambda/2 clip, obliquity with the 1e-16 horizon floor
+// and the centre-frequency sinc (_pfield_math.py:70-118, :165-199), and the MUFU recurrence
+// step (its ~4e-7 error compounds over at most seven steps).  Computed once per
+// (scatterer, source) by tc_geometry_kernel; returns (clipped r, amplitude, step).
+__device__ __forceinline__ float4 tc_geometry(float xs, float zs, float4 sp, float2 rot, const SweepConst& C) {
   const float dx = __fsub_rn(__fsub_rn(xs, sp.x), sp.y);
   const float dz = __fsub_rn(__fsub_rn(zs, sp.z), sp.w);
   const float d2 = fmaf(dx, dx, dz * dz);
@@ -76,17 +75,30 @@ __device__ __forceinline__ void tc_source(float xs, float zs, float4 sp, float2 
   const float x = C.dir_coef * sth;
   const float dir = (fabsf(x) < 1e-4f) ? 1.0f : __fdividef(__sinf(x), x);
   const float amp = ob * dir * rsqrtf(rc) * C.inv_nsub;
+  float sn, cs;
+  __sincosf(C.dk.x * rc, &sn, &cs);
+  const float mag = __expf(-C.dalpha * rc);
+  return make_float4(rc, amp, mag * cs, mag * sn);
+}
+
+// Anchor value amp exp(-a0 r) exp(i k0 r) at a band's first frequency, with k0 r reduced
+// mod 2 pi in FP32 (error ~1e-7 |k0 r|, below 1e-4 rad here).
+__device__ __forceinline__ float2 tc_anchor(float rc, float amp, float2 k0, float a0) {
   const float p = k0.x * rc;
   const float n = rintf(p * kInvTwoPi);
   const float ph = fmaf(-n, kTwoPiLo, fmaf(-n, kTwoPiHi, p));
   float sn, cs;
   __sincosf(ph, &sn, &cs);
   const float m = amp * __expf(-a0 * rc);
-  g = make_float2(m * cs, m * sn);
-  __sincosf(C.dk.x * rc, &sn, &cs);
-  const float mag = __expf(-C.dalpha * rc);
-  st = make_float2(mag * cs, mag * sn);
+  return make_float2(m * cs, m * sn);
 }
+
+// Generation mapping shared by the geometry pre-pass and the sweep: thread tid owns scatterer
+// s_g of a 64-scatterer tile and elements [16 eg, 16 eg + 16).  The eight lanes of a
+// quarter-warp share eg and take eight consecutive scatterers, so their 16-byte stores into
+// the core-matrix operand layouts fill one contiguous 128-byte row of banks.
+__device__ __forceinline__ int tc_sg(int tid) { return (tid >> 5) * 8 + (tid & 7); }
+__device__ __forceinline__ int tc_eg(int tid) { return (tid >> 3) & 3; }
 
 // SMEM layout (bytes).
 constexpr uint32_t kOffAtxHi = 0;                 // K-major  128 x 64 bf16
@@ -135,10 +147,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
   float* X = reinterpret_cast<float*>(sm + kOffX);
   float4* stage = reinterpret_cast<float4*>(sm + kOffAtxHi);  // geometry staging (A_tx region)
 
-  // generation mapping: scatterer s_g of the tile, elements [16 eg, 16 eg + 16).  The eight
-  // lanes of a quarter-warp share eg and take eight consecutive scatterers, so their 16-byte
-  // stores into the core-matrix operand layouts fill one contiguous 128-byte row of banks.
-  const int s_g = (tid >> 5) * 8 + (tid & 7), eg = (tid >> 3) & 3;
+  const int s_g = tc_sg(tid), eg = tc_eg(tid);
   // TMEM read mapping: lane quarter q (rows 32q..32q+31), column half h
   const int q = warp & 3, h = warp >> 2;
 
@@ -215,33 +224,18 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
         }
         rcs[s_g] = w;
       }
-      // ---- geometry of 16 elements x U sub-elements, 8 states at a time through shared memory ----
+      // ---- the tile's cached geometry (16 elements x U sub-elements per thread) -> anchors ----
       float2 G[16 * U], S[16 * U];
       {
-        const int64_t si = sval ? s : t0;
-        const float xs = (float)P.scat[2 * si];
-        const float zs = (float)P.scat[2 * si + 1];
+        const float4* gp = A.geo + ((P.tile0 + t0 / kTcT) * (16 * U)) * kThreads + tid;
 #pragma unroll
-        for (int c = 0; c < 2 * U; ++c) {
-#pragma unroll 4
-          for (int i = 0; i < 8; ++i) {
-            const int idx = c * 8 + i;  // state index j * U + u
-            const int e = eg * 16 + idx / U, u = idx % U;
-            const int ec = e < E ? e : E - 1;
-            float2 g, st;
-            tc_source(xs, zs, A.src_pos[ec * U + u], A.rot_e[ec], C, k0, a0, g, st);
-            const bool on = sval && e < E;
-            stage[i * kThreads + tid] = on ? make_float4(g.x, g.y, st.x, st.y) : make_float4(0.f, 0.f, 0.f, 0.f);
-          }
-#pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            const float4 v = stage[i * kThreads + tid];
-            G[c * 8 + i] = make_float2(v.x, v.y);
-            S[c * 8 + i] = make_float2(v.z, v.w);
-          }
+        for (int i = 0; i < 16 * U; ++i) {
+          const float4 v = gp[(size_t)i * kThreads];
+          G[i] = tc_anchor(v.x, v.y, k0, a0);
+          S[i] = make_float2(v.z, v.w);
         }
       }
-      __syncthreads();  // staging area (A_tx region) is reused below; rcs visible
+      __syncthreads();  // rcs visible
       const float rc_s = rcs[s_g];
 
       for (int f = 0; f < nf; ++f) {
@@ -474,6 +468,42 @@ __global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const float* Ag, co
   if (warp == 0) tc::tmem_dealloc(tmem, 64);
 }
 
+// Geometry of every (scatterer, source) of every phantom, once per sweep: one CTA per
+// (tile, phantom); thread tid writes its 16 U states (clipped r, amplitude, step) at
+// geo[((tile0 + tile) 16U + i) 256 + tid], so that the sweep's loads are coalesced.  Sources
+// of padded elements and scatterers past the end get zeros (no contribution).
+template <int U>
+__global__ void __launch_bounds__(kThreads) tc_geometry_kernel(const __grid_constant__ TcArgs A) {
+  const BatchPhantom& P = A.ph[blockIdx.y];
+  const int tid = threadIdx.x, s_g = tc_sg(tid), eg = tc_eg(tid);
+  const int64_t n_tiles = (P.n_scat + kTcT - 1) / kTcT;
+  SweepConst C = A.C;
+  C.dk = P.dk;
+  C.dalpha = P.dalpha;
+  for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    const int64_t s = t * kTcT + s_g;
+    const bool sval = s < P.n_scat;
+    const int64_t si = sval ? s : t * kTcT;
+    const float xs = (float)P.scat[2 * si], zs = (float)P.scat[2 * si + 1];
+    float4* gp = const_cast<float4*>(A.geo) + ((P.tile0 + t) * (16 * U)) * kThreads + tid;
+#pragma unroll 4
+    for (int i = 0; i < 16 * U; ++i) {
+      const int e = eg * 16 + i / U, u = i % U;
+      const int ec = e < A.E ? e : A.E - 1;
+      const float4 v = tc_geometry(xs, zs, A.src_pos[ec * U + u], A.rot_e[ec], C);
+      gp[(size_t)i * kThreads] = (sval && e < A.E) ? v : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+}
+
+cudaError_t launch_tc_geometry(int U, int max_tiles, int sms, const TcArgs& A, cudaStream_t s) {
+  const int gx = max_tiles < 4 * sms ? max_tiles : 4 * sms;
+  const dim3 grid(gx > 0 ? gx : 1, A.n_phantoms);
+  if (U == 1) tc_geometry_kernel<1><<<grid, kThreads, 0, s>>>(A);
+  else tc_geometry_kernel<2><<<grid, kThreads, 0, s>>>(A);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_tc(int U, int grid, const TcArgs& A, cudaStream_t s) {
   const uint32_t smem = tc_smem_bytes(A.fb);
   cudaError_t e;
@@ -502,9 +532,10 @@ using namespace fsg;
 size_t tc_a256(size_t v) { return (v + 255) & ~size_t(255); }
 
 struct TcLayout {
-  int fb, chunk, n_items;
+  int fb, chunk, n_items, max_tiles;
   int n_bands[kMaxPhantoms], n_chunks[kMaxPhantoms], item0[kMaxPhantoms];
-  size_t off_src, off_rot, off_tau, off_apod, off_queue, off_tab[kMaxPhantoms], off_partial, total;
+  int64_t tile0[kMaxPhantoms];
+  size_t off_src, off_rot, off_tau, off_apod, off_queue, off_tab[kMaxPhantoms], off_partial, off_geo, total;
 };
 
 void tc_layout(const FsgProbe* probe, const FsgPhantom* ph, int n_ph, int n_tx, const FsgBatchTuning* tu,
@@ -512,7 +543,9 @@ void tc_layout(const FsgProbe* probe, const FsgPhantom* ph, int n_ph, int n_tx, 
   int fb = (tu && tu->freqs_per_item > 0) ? tu->freqs_per_item : 7;
   if (fb > kTcMaxFb) fb = kTcMaxFb;
   L->fb = fb;
-  int64_t chunk = (tu && tu->chunk_scatterers > 0) ? tu->chunk_scatterers : 65536;
+  // the items of one chunk run side by side, so a chunk's geometry (16 KB per scatterer at
+  // U = 2) should stay resident in L2: 16,384 scatterers by default
+  int64_t chunk = (tu && tu->chunk_scatterers > 0) ? tu->chunk_scatterers : 16384;
   chunk = ((chunk + kTcT - 1) / kTcT) * kTcT;
   L->chunk = (int)chunk;
   const int E = probe->n_elements, U = probe->n_sub;
@@ -523,6 +556,8 @@ void tc_layout(const FsgProbe* probe, const FsgPhantom* ph, int n_ph, int n_tx, 
   L->off_apod = o; o += tc_a256((size_t)n_tx * E * 4);
   L->off_queue = o; o += 256;  // queue counter + status word
   int items = 0;
+  int64_t tiles = 0;
+  L->max_tiles = 0;
   for (int p = 0; p < n_ph; ++p) {
     const int F = ph[p].plan.n_freq;
     L->n_bands[p] = (F + fb - 1) / fb;
@@ -531,10 +566,16 @@ void tc_layout(const FsgProbe* probe, const FsgPhantom* ph, int n_ph, int n_tx, 
     items += L->n_bands[p] * L->n_chunks[p];
     L->off_tab[p] = o;
     o += tc_a256((size_t)F * (8 + 4 + 8 + 8 + 4));
+    L->tile0[p] = tiles;
+    const int64_t t = (ph[p].n_scat + kTcT - 1) / kTcT;
+    tiles += t;
+    if (t > L->max_tiles) L->max_tiles = (int)t;
   }
   L->n_items = items;
   L->off_partial = o;
   o += tc_a256((size_t)items * fb * kTcTx * kTcE * 8);
+  L->off_geo = o;
+  o += tc_a256((size_t)tiles * 16 * U * kThreads * 16);
   L->total = o;
 }
 
@@ -613,6 +654,7 @@ extern "C" int32_t fsg_simus_batched_tc(const FsgProbe* probe, const FsgMedium* 
     b.n_bands = L.n_bands[p];
     b.n_chunks = L.n_chunks[p];
     b.item0 = L.item0[p];
+    b.tile0 = L.tile0[p];
     b.f0 = q.plan.freq_start;
     b.df = q.plan.freq_step;
     b.corr = (float)q.plan.correction_factor;
@@ -671,6 +713,9 @@ extern "C" int32_t fsg_simus_batched_tc(const FsgProbe* probe, const FsgMedium* 
     A.queue = queue;
     A.status = queue + 1;
     A.partial = partial;
+    A.geo = reinterpret_cast<const float4*>(ws + L.off_geo);
+    if ((st = check_cuda(launch_tc_geometry(U, L.max_tiles, sms, A, s), "tc_geometry_kernel launch")) != FSG_OK)
+      return st;
     int grid = sms;
     if (grid > L.n_items) grid = L.n_items;
     if ((st = check_cuda(launch_tc(U, grid, A, s), "tc_kernel launch")) != FSG_OK) return st;
