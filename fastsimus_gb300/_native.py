@@ -50,6 +50,11 @@ class FsgPhantom(ctypes.Structure):
                 ("plan", FsgFreqPlan), ("out", ctypes.c_void_p)]
 
 
+class FsgMlpWeights(ctypes.Structure):
+    _fields_ = [("packed", ctypes.c_void_p * 4), ("bias", ctypes.c_void_p * 4), ("w_head", ctypes.c_void_p),
+                ("b_head", ctypes.c_void_p), ("bmat", ctypes.c_void_p)]
+
+
 class FsgBatchTuning(ctypes.Structure):
     _fields_ = [("freqs_per_item", ctypes.c_int32), ("chunk_scatterers", ctypes.c_int32),
                 ("ctas_per_sm", ctypes.c_int32), ("reserved0", ctypes.c_int32)]
@@ -103,6 +108,9 @@ _SIGNATURES = {
     "fsg_fp32_fma_probe": (ctypes.c_int32, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
                                             _P]),
     "fsg_rf_workspace_size": (ctypes.c_size_t, [ctypes.c_int32, ctypes.c_int32]),
+    "fsg_mlp_tc_packed_bytes": (ctypes.c_size_t, [ctypes.c_int32]),
+    "fsg_mlp_tc_pack": (ctypes.c_int32, [_P, ctypes.c_int32, ctypes.c_int32, _P, _P]),
+    "fsg_mlp_tc_forward": (ctypes.c_int32, [ctypes.POINTER(FsgMlpWeights), _P, ctypes.c_int64, _P, _P, _P]),
     "fsg_irfft_gate": (ctypes.c_int32, [_P, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
                                         ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P,
                                         ctypes.c_size_t, _P]),

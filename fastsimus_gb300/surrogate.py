@@ -150,6 +150,43 @@ class TxFieldSurrogate:
         self._gemm(x, HIDDEN, 1, self.Wb[DEPTH], 1, HIDDEN, 1, self.b[DEPTH], None, out, None, 2, n, 2, HIDDEN, 0)
         return out, (acts, zs)
 
+    # -- tensor-core inference ------------------------------------------------------------------
+    def _tc_weights(self):
+        """Packed BF16 hidden-layer weights for ``fsg_mlp_tc_forward``; re-packed after every
+        optimiser step."""
+        if getattr(self, "_tc_step", None) != self.step:
+            lib, stream = self.lib, self._stream()
+            self._tc_packed = []
+            for layer in range(DEPTH):
+                k = self.Wb[layer].shape[1]
+                buf = torch.empty(lib.fsg_mlp_tc_packed_bytes(k) // 2, dtype=torch.bfloat16, device=self.device)
+                _check(lib.fsg_mlp_tc_pack(self.Wb[layer].data_ptr(), HIDDEN, k, buf.data_ptr(), stream))
+                self._tc_packed.append(buf)
+            self._tc_head = self.Wb[DEPTH].float().contiguous()  # the head multiplies the same BF16 values
+            w = _native.FsgMlpWeights()
+            for layer in range(DEPTH):
+                w.packed[layer] = self._tc_packed[layer].data_ptr()
+                w.bias[layer] = self.b[layer].data_ptr()
+            w.w_head = self._tc_head.data_ptr()
+            w.b_head = self.b[DEPTH].data_ptr()
+            w.bmat = self.bmat.data_ptr()
+            self._tc_struct = w
+            self._tc_status = torch.zeros(1, dtype=torch.int32, device=self.device)
+            self._tc_step = self.step
+        return self._tc_struct
+
+    def forward_tc(self, u: torch.Tensor) -> torch.Tensor:
+        """The network's output (n x 2) by the fused tcgen05 kernel (inference only)."""
+        w = self._tc_weights()
+        u = u.contiguous()
+        out = torch.empty(u.shape[0], 2, device=self.device)
+        _check(self.lib.fsg_mlp_tc_forward(ctypes.byref(w), u.data_ptr(), u.shape[0], out.data_ptr(),
+                                           self._tc_status.data_ptr(), self._stream()))
+        return out
+
+    def tc_status(self) -> int:
+        return int(self._tc_status.item()) if hasattr(self, "_tc_status") else 0
+
     def backward(self, cache, dout: torch.Tensor):
         acts, zs = cache
         n = dout.shape[0]
@@ -235,11 +272,14 @@ class TxFieldSurrogate:
                 "samples": n_train, "scale": self.scale}
 
     @torch.no_grad()
-    def predict(self, samples: torch.Tensor, chunk: int = 1 << 20) -> torch.Tensor:
+    def predict(self, samples: torch.Tensor, chunk: int = 1 << 20, backend: str = "tc") -> torch.Tensor:
+        """Complex transmit pressure at samples (n, 4) [x, z, f, theta].  ``backend="tc"`` runs
+        the fused tensor-core forward pass, ``"simt"`` the training kernels' forward pass."""
         out = torch.empty(samples.shape[0], dtype=torch.complex64, device=self.device)
         for i in range(0, samples.shape[0], chunk):
             s = samples[i:i + chunk]
-            o, _ = self.forward(self.normalise(s))
+            u = self.normalise(s)
+            o = self.forward_tc(u) if backend == "tc" else self.forward(u)[0]
             out[i:i + chunk] = torch.view_as_complex(o.contiguous()) * self.scale * self.carrier(s)
         return out
 

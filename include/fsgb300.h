@@ -256,6 +256,28 @@ int32_t fsg_simus_noalloc(const FsgProbe* probe, const FsgMedium* medium, const 
 size_t fsg_simus_noalloc_scratch_bytes(void);
 
 /*
+ * Tensor-core inference of the transmit-field surrogate network (no counterpart in the
+ * reference).  Network: features [sin(2 pi B u), cos(2 pi B u)] (B: 64 x 4, row-major) of the
+ * normalised inputs u (n x 4), hidden layers 128 -> 256 -> 256 -> 256 -> 256 with SiLU, head
+ * 256 -> 2.  packed[l]: hidden layer l's [256][K] BF16 weights rearranged by fsg_mlp_tc_pack
+ * (fsg_mlp_tc_packed_bytes(K) bytes); bias[l]: 256 floats; w_head: [2][256] floats; b_head: 2.
+ * out: n x 2 floats.  status: device int set to FSG_ETIMEOUT if a bounded wait gave up (the
+ * caller zeroes it).
+ */
+typedef struct FsgMlpWeights {
+  const void* packed[4];
+  const float* bias[4];
+  const float* w_head;
+  const float* b_head;
+  const float* bmat;
+} FsgMlpWeights;
+
+size_t fsg_mlp_tc_packed_bytes(int32_t n_in);
+int32_t fsg_mlp_tc_pack(const void* w_bf16, int32_t n_out, int32_t n_in, void* packed, void* stream);
+int32_t fsg_mlp_tc_forward(const FsgMlpWeights* weights, const float* u, int64_t n, float* out, int32_t* status,
+                           void* stream);
+
+/*
  * Spectrum -> RF epilogue.  Replaces _irfft_and_threshold (simus.py:336-367):
  *   rf = irfft(conj(spectrum), n_fft, axis 0)[: (n_fft + 1) / 2]
  *   rf *= 0.5 (1 + tanh((|rf| / max|rf| - 1e-5) / 1e-6))        (when gate != 0)

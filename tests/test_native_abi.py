@@ -48,4 +48,5 @@ def test_struct_layouts_match_header():
     assert _native.FsgProbe.baffle_impedance.offset == 48
     assert ctypes.sizeof(_native.FsgMedium) == 16
     assert ctypes.sizeof(_native.FsgFreqPlan) == 64
+    assert ctypes.sizeof(_native.FsgMlpWeights) == 11 * 8
     assert _native.FsgFreqPlan.pulse_spectrum.offset == 48

@@ -73,6 +73,30 @@ def test_network_gradients_match_fp64_oracle():
         assert G.rel_l2(a.double().cpu().numpy(), r) < 1e-4
 
 
+def test_tc_forward_matches_training_forward():
+    """The fused tcgen05 inference kernel (BF16 weights, hi + lo BF16 activations, FP32
+    accumulation in TMEM) against the training kernels' FP32-activation forward pass."""
+    sur = _surrogate(seed=6)
+    for n in (1000, 128, 1):  # ragged last tile, exactly one tile, a single query
+        s = sur.sample_domain(n, seed=9 + n)
+        u = sur.normalise(s)
+        ref, _ = sur.forward(u)
+        got = sur.forward_tc(u)
+        torch.cuda.synchronize()
+        assert sur.tc_status() == 0
+        err = G.rel_l2(got.double().cpu().numpy(), ref.double().cpu().numpy())
+        print(f"tc forward n={n}: relL2 vs training forward {err:.2e}")
+        assert err < 1e-4
+    # after an optimiser step the packed weights follow the new values
+    y = torch.zeros(256, 2, device=sur.device)
+    u = sur.normalise(sur.sample_domain(256, seed=3))
+    _, gW, gb = sur.loss_and_grads(u, y)
+    sur.adam(gW, gb, 1e-2)
+    ref, _ = sur.forward(u)
+    got = sur.forward_tc(u)
+    assert G.rel_l2(got.double().cpu().numpy(), ref.double().cpu().numpy()) < 1e-4
+
+
 def test_training_reduces_error():
     sur = _surrogate(seed=1)
     rep = sur.train(n_train=40960, epochs=4, batch=2048, lr=3e-3, n_val=4096)
