@@ -751,17 +751,21 @@ def run_surrogate_workload(args):
     q = sur.sample_domain(1 << 20, seed=9)
     for _ in range(2):
         sur.predict(q)
+        sur.predict(q, backend="simt")
         sur.exact(q)
     torch.cuda.synchronize()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     ev[0].record()
-    pred = sur.predict(q)
+    pred = sur.predict(q)  # fused tcgen05 forward pass
     ev[1].record()
     ex = sur.exact(q)
     ev[2].record()
+    sur.predict(q, backend="simt")  # the training kernels' forward pass
+    ev[3].record()
     torch.cuda.synchronize()
     t_net_q = ev[0].elapsed_time(ev[1]) * 1e-3 / q.shape[0]
     t_exact_q = ev[1].elapsed_time(ev[2]) * 1e-3 / q.shape[0]
+    t_net_simt_q = ev[2].elapsed_time(ev[3]) * 1e-3 / q.shape[0]
     val_rel = float(torch.linalg.vector_norm(pred - ex) / torch.linalg.vector_norm(ex))
     # the 1M x 75 use case
     full_s, full_rc = W.cfg4_scatterers(1_000_000, seed=1)
@@ -786,7 +790,8 @@ def run_surrogate_workload(args):
     line = {
         "metric": "RF frames/s & Green terms/s: surrogate (with exact fallback at 1e-3) vs exact FP32 path",
         "value": frames / t_sur_full, "unit": "frames/s", "n_gpus": 1, "higher_is_better": True,
-        "dtype": "bf16 weights, f32 accumulate (network); f32 exact fallback", "data": "synthetic (seeded)",
+        "dtype": "bf16 weights, bf16 hi/lo activations, f32 accumulate (tcgen05 network); f32 exact fallback",
+        "data": "synthetic (seeded)",
         "config": {"workload": "cfg5: cfg1 probe; train 2M samples (x, z, f, theta) over the cfg1 box, "
                                "fc(1 +- B/2), +-16 deg; use 1,000,000 scatterers x 75 plane waves",
                    "train_samples": args.sur_train, "epochs": args.sur_epochs,
@@ -795,7 +800,9 @@ def run_surrogate_workload(args):
                      "final_train_mse": rep["history"][-1]["train_mse"],
                      "val_rel_l2": rep["history"][-1]["val_rel_l2"], "history": rep["history"]},
         "field_rel_l2_1M_queries": val_rel,
-        "per_query_s": {"network": t_net_q, "exact_kernel": t_exact_q, "ratio_network_over_exact": t_net_q / t_exact_q},
+        "per_query_s": {"network": t_net_q, "network_simt_forward": t_net_simt_q, "exact_kernel": t_exact_q,
+                        "ratio_network_over_exact": t_net_q / t_exact_q,
+                        "network_tc_status": sur.tc_status()},
         "simus_1M_x75": {
             "surrogate_s_scaled": t_sur_full, "exact_fp32_batched_s": t_exact_full,
             "gain_vs_exact": t_exact_full / t_sur_full,

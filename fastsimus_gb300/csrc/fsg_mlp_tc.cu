@@ -82,9 +82,29 @@ __global__ void __launch_bounds__(256, 1) mlp_tc_forward_kernel(const __grid_con
   const uint32_t tmem = tmem_holder;
   const uint32_t sbase = tc::smem_u32(sm);
   const uint32_t idesc = tc::idesc_bf16(kMlpRows, kMlpWidth, 0, 0);
-  // thread 0's mbarrier bookkeeping: chunks issued / consumed per buffer, layer phase
+  // Thread 0 streams the weights as one sequence of 32 KB chunks over all layers and tiles
+  // (kChunksPerTile per tile), keeping up to two in flight; chunk g goes to buffer g & 1.
+  constexpr int kChunksPerTile = kMlpFeat / kMlpChunkK + 3 * (kMlpWidth / kMlpChunkK);
   uint32_t ph_full[2] = {0u, 0u}, ph_free[2] = {0u, 0u}, ph_layer = 0u;
-  int used[2] = {0, 0};
+  int64_t next_load = 0;  // next chunk to copy
+  const int64_t my_tiles = ((n + kMlpRows - 1) / kMlpRows - blockIdx.x + gridDim.x - 1) / gridDim.x;
+  const int64_t total_chunks = my_tiles * kChunksPerTile;
+  // issue the copy of chunk g; before reusing a buffer, wait for the MMAs of chunk g - 2
+  auto load = [&](int64_t g) -> bool {
+    const int b = (int)(g & 1);
+    if (g >= 2) {
+      if (!tc::mbar_wait_bounded(&mbar_free[b], ph_free[b], kMlpWaitTries)) return false;
+      ph_free[b] ^= 1u;
+    }
+    const int j = (int)(g % kChunksPerTile);
+    const int layer = j < 2 ? 0 : 1 + (j - 2) / 4, c = j < 2 ? j : (j - 2) % 4;
+    tc::mbar_arrive_expect_tx(&mbar_full[b], kMlpChunkBytes);
+    tc::bulk_g2s(sm + (b ? kOffB1 : kOffB0),
+                 static_cast<const unsigned char*>(W.packed[layer]) + (size_t)c * kMlpChunkBytes, kMlpChunkBytes,
+                 &mbar_full[b]);
+    return true;
+  };
+  int64_t tile_iter = 0;
 
   // TMEM read mapping: row = 32 (warp % 4) + lane, columns [128 (warp / 4), +128)
   const int row = 32 * (warp & 3) + lane, chalf = warp >> 2;
@@ -116,27 +136,17 @@ __global__ void __launch_bounds__(256, 1) mlp_tc_forward_kernel(const __grid_con
     tc::fence_after_sync();
 
     float2 head = make_float2(0.f, 0.f);
+    int64_t chunk0 = tile_iter * kChunksPerTile;  // global index of this layer's first chunk
     for (int layer = 0; layer < 4; ++layer) {
       const int K = layer == 0 ? kMlpFeat : kMlpWidth;
       const int nch = K / kMlpChunkK;
-      const unsigned char* wl = static_cast<const unsigned char*>(W.packed[layer]);
-      // ---- MMAs: thread 0 streams the weight chunks and issues the products ----
+      // ---- MMAs: thread 0 keeps two weight chunks in flight and issues the products ----
       if (tid == 0 && !s_fail) {
-        auto load = [&](int c) -> bool {
-          const int b = c & 1;
-          if (used[b]) {  // the MMAs that read this buffer must be done
-            if (!tc::mbar_wait_bounded(&mbar_free[b], ph_free[b], kMlpWaitTries)) return false;
-            ph_free[b] ^= 1u;
-          }
-          tc::mbar_arrive_expect_tx(&mbar_full[b], kMlpChunkBytes);
-          tc::bulk_g2s(sm + (b ? kOffB1 : kOffB0), wl + (size_t)c * kMlpChunkBytes, kMlpChunkBytes, &mbar_full[b]);
-          used[b] = 1;
-          return true;
-        };
-        bool ok = load(0);
+        bool ok = true;
         for (int c = 0; c < nch && ok; ++c) {
-          const int b = c & 1;
-          if (c + 1 < nch) ok = load(c + 1);
+          const int64_t g = chunk0 + c;
+          const int b = (int)(g & 1);
+          while (ok && next_load < g + 2 && next_load < total_chunks) ok = load(next_load++);
           if (!ok) break;
           if (!tc::mbar_wait_bounded(&mbar_full[b], ph_full[b], kMlpWaitTries)) { ok = false; break; }
           ph_full[b] ^= 1u;
@@ -158,8 +168,12 @@ __global__ void __launch_bounds__(256, 1) mlp_tc_forward_kernel(const __grid_con
           ok = tc::mbar_wait_bounded(&mbar_layer, ph_layer, kMlpWaitTries);
           ph_layer ^= 1u;
         }
+        // the layer's products are done and both buffers are free: start the next two
+        // copies now, so that they land while the epilogue runs
+        while (ok && next_load < chunk0 + nch + 2 && next_load < total_chunks) ok = load(next_load++);
         if (!ok) s_fail = 1;
       }
+      chunk0 += nch;
       tc::fence_before_sync();
       __syncthreads();
       tc::fence_after_sync();
@@ -202,6 +216,7 @@ __global__ void __launch_bounds__(256, 1) mlp_tc_forward_kernel(const __grid_con
       }
     }
     __syncthreads();
+    ++tile_iter;
   }
   tc::fence_before_sync();
   __syncthreads();
