@@ -100,3 +100,19 @@ def test_batched_rejects_unsupported_shapes():
     s, r = W.cfg2_scatterers(100)
     with pytest.raises(NotImplementedError):
         BatchedSimus([(s, r)], np.zeros((2, 128)), p2, m2).run()
+
+
+def test_batched_phantom_without_scatterers_gives_zero():
+    """A phantom with no scatterers next to a populated one: zero RF for it, unchanged RF
+    for the other."""
+    from fastsimus_gb300 import workloads as W
+    from fastsimus_gb300.batched import BatchedSimus
+
+    p, m = W.cfg1_probe(), W.cfg1_medium()
+    s, r = W.cfg1_scatterers(500, seed=3)
+    empty = (np.zeros((0, 2)), np.zeros(0))
+    delays = W.plane_wave_delays(p, m, [-5.0, 5.0])
+    both = BatchedSimus([(s, r), empty], delays, p, m).run()
+    alone = BatchedSimus([(s, r)], delays, p, m).run()
+    assert float(np.abs(np64(both[1].rf)).max()) == 0.0
+    assert G.rel_l2(np64(both[0].rf), np64(alone[0].rf)) < 1e-6
