@@ -63,7 +63,6 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
   float2* W = D + FB * kBE * kWPitch;                                // [kBT][kWPitch]
   float* rcs = reinterpret_cast<float*>(W + kBT * kWPitch);          // [kBT]
   __shared__ int s_item;
-  __shared__ float4 xz[kBT];  // the tile's scatterer coordinates as double-float (x hi, x lo, z hi, z lo)
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wm = warp & 3, wn = warp >> 2, lm = lane & 3, ln = lane >> 2;
@@ -121,20 +120,16 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
         for (int j = 0; j < 5; ++j) Y[f][i][j] = make_float2(0.f, 0.f);
 
     for (int64_t t0 = s_begin; t0 < s_end; t0 += kBT) {
-      // --- the tile's coordinates (split once per scatterer) and reflectivities ---
+      // --- the tile's reflectivities (0 out of field) ---
       if (tid < kBT) {
         const int64_t s = t0 + tid;
         float w = 0.f;
-        float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
         if (s < s_end) {
           const double x = P.scat[2 * s], z = P.scat[2 * s + 1];
-          const dfl hx = split_double(x), hz = split_double(z);
-          c = make_float4(hx.hi, hx.lo, hz.hi, hz.lo);
           bool out = z < 0.0;
           if (A.convex) out = out || (x * x + (z + A.apex) * (z + A.apex) <= A.radius2);
           w = out ? 0.f : (float)P.rc[s];
         }
-        xz[tid] = c;
         rcs[tid] = w;
       }
       __syncthreads();
@@ -147,15 +142,13 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
           const int64_t s = t0 + sl;
           float2 g0 = make_float2(0.f, 0.f), g1 = make_float2(0.f, 0.f);
           if (e < E && s < s_end) {
-            const float4 c = xz[sl];
-            const dfl xs{c.x, c.y}, zs{c.z, c.w};
-            const float2 rot = A.rot_e[e];
+            // cached geometry of (s, e, u): the U records of a thread are contiguous
+            const int64_t rec = (P.geo0 + s) * (int64_t)(E * U) + e * U;
             for (int u = 0; u < U; ++u) {
-              const int src = e * U + u;
-              const SrcGeo geo = source_geometry(xs, zs, A.src_pos[src], rot, C);
-              const float2 a = anchor_value(geo.r_hi, geo.r_lo, geo.amp, k0, a0);
+              const float4 ga = A.geo_a[rec + u];
+              const float2 a = anchor_value(ga.x, ga.y, ga.z, k0, a0);
               g0 = cadd(g0, a);
-              if (FB > 1) g1 = cadd(g1, cmul(a, geo.step));
+              if (FB > 1) g1 = cadd(g1, cmul(a, make_float2(ga.w, A.geo_b[rec + u])));
             }
           }
           Gm[sl * kGmPitch + e] = g0;
@@ -292,6 +285,39 @@ __global__ void batched_reduce(const __grid_constant__ BatchReduceArgs a) {
   }
 }
 
+// Geometry of every (scatterer, source) of every phantom, once per sweep (the FP32 path keeps
+// the plain kernels' double-float distance and accurate step, so the cache carries r as a
+// double-float pair).  A CTA takes `spb` scatterers at a time: their coordinates are split
+// once into shared memory, then consecutive threads write consecutive sources.
+__global__ void __launch_bounds__(kThreads) batched_geometry_kernel(const __grid_constant__ BatchArgs A) {
+  __shared__ float4 xz[kThreads];
+  const BatchPhantom& P = A.ph[blockIdx.y];
+  const int n_src = A.E * A.U;
+  const int spb = n_src >= kThreads ? 1 : kThreads / n_src;
+  SweepConst C = A.C;
+  C.dk = P.dk;
+  C.dalpha = P.dalpha;
+  for (int64_t s0 = (int64_t)blockIdx.x * spb; s0 < P.n_scat; s0 += (int64_t)gridDim.x * spb) {
+    __syncthreads();
+    if (threadIdx.x < spb && s0 + threadIdx.x < P.n_scat) {
+      const int64_t s = s0 + threadIdx.x;
+      const dfl hx = split_double(P.scat[2 * s]), hz = split_double(P.scat[2 * s + 1]);
+      xz[threadIdx.x] = make_float4(hx.hi, hx.lo, hz.hi, hz.lo);
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < spb * n_src; it += blockDim.x) {
+      const int sl = it / n_src, src = it % n_src;
+      const int64_t s = s0 + sl;
+      if (s >= P.n_scat) continue;
+      const float4 c = xz[sl];
+      const SrcGeo g = source_geometry(dfl{c.x, c.y}, dfl{c.z, c.w}, A.src_pos[src], A.rot_e[src / A.U], C);
+      const int64_t rec = (P.geo0 + s) * (int64_t)n_src + src;
+      A.geo_a[rec] = make_float4(g.r_hi, g.r_lo, g.amp, g.step.x);
+      A.geo_b[rec] = g.step.y;
+    }
+  }
+}
+
 size_t batched_smem_bytes(int fb) {
   return (size_t)(fb * kBT * kGmPitch + fb * kBE * kWPitch + kBT * kWPitch) * sizeof(float2) + kBT * sizeof(float);
 }
@@ -326,7 +352,9 @@ size_t a256(size_t v) { return (v + 255) & ~size_t(255); }
 struct BatchPlanLayout {
   int fb, chunk, n_items;
   int n_bands[kMaxPhantoms], n_chunks[kMaxPhantoms], item0[kMaxPhantoms];
-  size_t off_src, off_rot, off_tau, off_apod, off_queue, off_tab[kMaxPhantoms], off_partial, total;
+  int64_t geo0[kMaxPhantoms], max_scat;
+  size_t off_src, off_rot, off_tau, off_apod, off_queue, off_tab[kMaxPhantoms], off_partial, off_geo_a, off_geo_b,
+      total;
 };
 
 int plan_layout(const FsgProbe* probe, const FsgPhantom* ph, int n_ph, int n_tx, const FsgBatchTuning* tu,
@@ -343,6 +371,8 @@ int plan_layout(const FsgProbe* probe, const FsgPhantom* ph, int n_ph, int n_tx,
   L->off_apod = o; o += a256((size_t)n_tx * E * 4);
   L->off_queue = o; o += 256;
   int items = 0;
+  int64_t scat = 0;
+  L->max_scat = 0;
   for (int p = 0; p < n_ph; ++p) {
     const int F = ph[p].plan.n_freq;
     L->n_bands[p] = (F + L->fb - 1) / L->fb;
@@ -351,10 +381,17 @@ int plan_layout(const FsgProbe* probe, const FsgPhantom* ph, int n_ph, int n_tx,
     items += L->n_bands[p] * L->n_chunks[p];
     L->off_tab[p] = o;
     o += a256((size_t)F * (8 + 4 + 8 + 8 + 4));
+    L->geo0[p] = scat;
+    scat += ph[p].n_scat;
+    if (ph[p].n_scat > L->max_scat) L->max_scat = ph[p].n_scat;
   }
   L->n_items = items;
   L->off_partial = o;
   o += a256((size_t)items * L->fb * kBTX * kBE * 8);
+  L->off_geo_a = o;
+  o += a256((size_t)scat * E * U * 16);
+  L->off_geo_b = o;
+  o += a256((size_t)scat * E * U * 4);
   L->total = o;
   return FSG_OK;
 }
@@ -449,6 +486,7 @@ static int32_t simus_batched_impl(const FsgProbe* probe, const FsgMedium* medium
     b.n_bands = L.n_bands[p];
     b.n_chunks = L.n_chunks[p];
     b.item0 = L.item0[p];
+    b.geo0 = L.geo0[p];
     b.f0 = q.plan.freq_start;
     b.df = q.plan.freq_step;
     b.corr = (float)q.plan.correction_factor;
@@ -509,6 +547,14 @@ static int32_t simus_batched_impl(const FsgProbe* probe, const FsgMedium* medium
     A.queue = queue;
     A.partial = partial;
     A.tx_in = tx_in;
+    A.geo_a = reinterpret_cast<float4*>(ws + L.off_geo_a);
+    A.geo_b = reinterpret_cast<float*>(ws + L.off_geo_b);
+    if (L.max_scat > 0) {
+      const int spb = E * U >= kThreads ? 1 : kThreads / (E * U);
+      const int64_t want = (L.max_scat + spb - 1) / spb, cap = (int64_t)sms * 8;
+      batched_geometry_kernel<<<dim3((unsigned)(want < cap ? want : cap), n_phantoms), kThreads, 0, s>>>(A);
+      if ((st = check_cuda(cudaGetLastError(), "batched_geometry_kernel launch")) != FSG_OK) return st;
+    }
     const int per_sm = (tuning && tuning->ctas_per_sm > 0) ? tuning->ctas_per_sm : 1;
     int grid = sms * per_sm;
     if (grid > L.n_items) grid = L.n_items;

@@ -17,6 +17,7 @@ struct BatchPhantom {
   const double* rc;         // [n_scat]
   int64_t n_scat;
   int64_t tile0;            // tensor-core path: this phantom's first tile in the geometry cache
+  int64_t geo0;             // FP32 batched path: this phantom's first scatterer in the geometry cache
   int n_freq, n_freq_full, freq_idx_start, n_bands, n_chunks, item0;
   double f0, df;
   float corr;
@@ -45,6 +46,10 @@ struct BatchArgs {
   int* queue;
   float2* partial;          // [n_items][fb][80][64]
   const float2* tx_in;      // optional [n_scat][n_freq][n_tx] transmit field (phantom 0); NULL = compute
+  // geometry of every (scatterer, source), computed once per sweep by batched_geometry_kernel:
+  // record (geo0 + s) * E * U + e * U + u holds (r_hi, r_lo, amp, step.x) and step.y
+  float4* geo_a;
+  float* geo_b;
 };
 
 struct BatchSetupArgs {
@@ -65,6 +70,7 @@ struct BatchReduceArgs {
 };
 
 size_t batched_smem_bytes(int fb);
+__global__ void batched_geometry_kernel(const __grid_constant__ BatchArgs A);
 cudaError_t launch_batched(int fb, int grid, const BatchArgs& A, cudaStream_t s);
 __global__ void batched_setup(const __grid_constant__ BatchSetupArgs a);
 __global__ void batched_reduce(const __grid_constant__ BatchReduceArgs a);
