@@ -215,10 +215,20 @@ static int choose_plane_pad(int E, int U, int gn, int st) {
 // Geometry cache per chunk: sized to stay resident in L2 while every band's CTAs read it.
 constexpr size_t kGeoCacheBudget = size_t(48) << 20;
 
-// Simus sweep shape.  The scatterers are processed in chunks of chunk_tiles tiles; a chunk is
-// split into n_slices contiguous slices of per_slice scatterers, one CTA row per slice.
-// cache_budget bounds the geometry cache (chunk_tiles * geo_bytes) from above; a chunk holds
-// at least one tile per slice.
+// Grid of one simus chunk: every (band, tile) unit is one CTA's work at most.
+static int simus_grid(int n_bands, int64_t chunk_tiles, int num_sms) {
+  const int64_t units = (int64_t)n_bands * chunk_tiles;
+  return (int)(units < num_sms ? units : num_sms);
+}
+
+// Simus sweep shape.  The scatterers are processed in chunks of chunk_tiles tiles, so that the
+// chunk's geometry cache (chunk_tiles * geo_bytes) stays below cache_budget.  A chunk's
+// n_bands x chunk_tiles (band, tile) units are split evenly over min(num_sms, units) CTAs in
+// band-major order: every SM gets the same work whatever the band count divides into, and a
+// CTA whose share crosses a band boundary sweeps two bands one after the other.  n_slices
+// bounds the number of CTAs that share a band (the partial-spectrum slots per band) for any
+// chunk size: a band's ct units hold fewer than ceil(grid / n_bands) CTA starts besides its
+// first unit's CTA.
 SweepConfig simus_config(int E, int U, int F, int64_t n_scat, int num_sms, size_t cache_budget, int ffd) {
   SweepConfig c;
   const int n_src = E * U;
@@ -233,18 +243,14 @@ SweepConfig simus_config(int E, int U, int F, int64_t n_scat, int num_sms, size_
   const SmemLayout L = smem_layout(c.st, c.fb, E, U, c.plane_pad, true, ffd != 0);
   c.smem = L.total;
   c.geo_bytes = L.geo_bytes;
+  c.per_slice = 0;
   const int64_t tiles = n_scat > 0 ? (n_scat + c.st - 1) / c.st : 1;
-  int64_t slices = num_sms / c.n_bands;
-  if (slices < 1) slices = 1;
-  if (slices > tiles) slices = tiles;
-  int64_t tps = (int64_t)(cache_budget / c.geo_bytes) / slices;  // tiles per slice and chunk
-  if (tps < 1) tps = 1;
-  const int64_t tps_all = (tiles + slices - 1) / slices;
-  if (tps > tps_all) tps = tps_all;
-  c.n_slices = (int)slices;
-  c.per_slice = tps * c.st;
-  c.chunk_tiles = tps * slices;
-  c.n_chunks = (tiles + c.chunk_tiles - 1) / c.chunk_tiles;
+  int64_t ct = (int64_t)(cache_budget / c.geo_bytes);
+  if (ct < 1) ct = 1;
+  if (ct > tiles) ct = tiles;
+  c.chunk_tiles = ct;
+  c.n_chunks = (tiles + ct - 1) / ct;
+  c.n_slices = 1 + (num_sms + c.n_bands - 1) / c.n_bands;
   return c;
 }
 
@@ -346,7 +352,6 @@ extern "C" int32_t fsg_simus(const FsgProbe* probe, const FsgMedium* medium, con
     A.pts = scat_xz;
     A.rc = rc;
     A.n_pts = n_scat;
-    A.per_slice = c.per_slice;
     A.t = t;
     A.C = make_sweep_const(probe, medium, plan, ffd);
     A.E = E;
@@ -363,12 +368,17 @@ extern "C" int32_t fsg_simus(const FsgProbe* probe, const FsgMedium* medium, con
     A.geo = geo;
     A.geo_bytes = c.geo_bytes;
     A.status = status;
+    A.n_bands = c.n_bands;
+    A.n_slots = c.n_slices;
+    if ((st = check_cuda(cudaMemsetAsync(partial, 0, (size_t)c.n_slices * F * E * 8, s), "partial reset")) != FSG_OK)
+      return st;
     const int64_t tiles = (n_scat + c.st - 1) / c.st;
     for (int64_t k = 0; k < c.n_chunks; ++k) {
       A.chunk_s0 = k * c.chunk_tiles * c.st;
-      A.accumulate = k > 0;
       const int64_t left = tiles - k * c.chunk_tiles;
       const int64_t ct = left < c.chunk_tiles ? left : c.chunk_tiles;
+      A.chunk_tiles = ct;
+      A.grid = simus_grid(c.n_bands, ct, sms);
       const int64_t cap = (int64_t)sms * 8;
       const int blocks = (int)(ct < cap ? ct : cap);
       geometry_kernel<<<blocks, kThreads, 0, s>>>(A, ct);

@@ -42,16 +42,26 @@ struct BandArgs {
   int plane_pad;       // extra words between the sub-element planes of the geometry arrays
   int convex;
   double apex, radius2;
-  void* partial;       // simus: float2 [slices][F][E]; pfield: float [bands][n_pts]
+  void* partial;       // simus: float2 [slots][F][E], zeroed, accumulated; pfield: float [bands][n_pts]
   // simus: scatterers are processed in chunks; the geometry of a chunk's tiles is computed
   // once by geometry_kernel into `geo` (one SmemLayout geometry block of geo_bytes per tile)
   // and copied into shared memory by each band's CTA with a TMA bulk copy
   unsigned char* geo;
   size_t geo_bytes;
   int64_t chunk_s0;    // first scatterer of the chunk (pts / rc are indexed globally)
-  int accumulate;      // add to the partial spectrum instead of overwriting it
+  // simus: the chunk's n_bands x chunk_tiles (band, tile) units are split evenly over `grid`
+  // CTAs in band-major order (cta_of_unit); the CTAs covering one band add into its partial
+  // slots 0, 1, ... (< n_slots) in CTA order
+  int64_t chunk_tiles;
+  int n_bands, n_slots, grid;
   int* status;         // FSG_ETIMEOUT when a bounded wait gave up
 };
+
+// The CTA whose share of the units [0, units) split over `grid` CTAs contains unit x.  CTA c
+// owns the units [c units / grid, (c + 1) units / grid).
+__host__ __device__ inline int cta_of_unit(int64_t x, int64_t units, int grid) {
+  return (int)(((x + 1) * grid - 1) / units);
+}
 
 struct SmemLayout {
   // Geometry arrays hold one value per (source, tile point): sub-element plane u, element e,
@@ -93,9 +103,10 @@ __host__ __device__ inline SmemLayout smem_layout(int st, int fb, int E, int U, 
 }
 
 struct SweepConfig {
-  int gn, st, fb, n_bands, n_slices, plane_pad;
-  int64_t per_slice;   // pfield: points per slice; simus: scatterers per slice within a chunk
-  int64_t chunk_tiles; // simus: tiles per chunk (a multiple of n_slices)
+  int gn, st, fb, n_bands, plane_pad;
+  int n_slices;        // pfield: point slices; simus: partial-spectrum slots per band
+  int64_t per_slice;   // pfield: points per slice
+  int64_t chunk_tiles; // simus: tiles per chunk
   int64_t n_chunks;
   size_t geo_bytes;    // simus: geometry block per tile
   size_t smem;

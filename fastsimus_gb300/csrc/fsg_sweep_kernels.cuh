@@ -190,6 +190,12 @@ struct SimusSink {
   }
 };
 
+// One CTA sweeps its share of the chunk's (band, tile) units: units [c W / G, (c + 1) W / G) of
+// W = n_bands x chunk_tiles in band-major order, i.e. one or two segments of consecutive tiles
+// of one band each.  Per segment: the band's tables into shared memory, then per tile the TMA
+// copy of the tile's geometry block, the transmit sums (tx_tile) into W, and the receive
+// accumulation of every element over the tile's scatterers; at the end of the segment the
+// running receive spectrum is added into the band's partial slot for this CTA.
 template <int U, int GN, bool FFD>
 __global__ void __launch_bounds__(kThreads, 1) simus_band_kernel(const BandArgs A) {
   extern __shared__ __align__(16) unsigned char sm[];
@@ -197,10 +203,6 @@ __global__ void __launch_bounds__(kThreads, 1) simus_band_kernel(const BandArgs 
   __shared__ uint64_t s_mbar;
   __shared__ int s_fail;
   const int tid = threadIdx.x;
-  const int f_b0 = blockIdx.x * A.fb;
-  const int64_t s_begin = A.chunk_s0 + (int64_t)blockIdx.y * A.per_slice;
-  const int64_t s_end = min(A.n_pts, s_begin + A.per_slice);
-  load_band_tables(A, L, sm, f_b0);
   if (tid == 0) {
     tc::mbar_init(&s_mbar, 1);
     tc::fence_mbar_init();
@@ -214,12 +216,6 @@ __global__ void __launch_bounds__(kThreads, 1) simus_band_kernel(const BandArgs 
   const int e_rx = tid % A.E;
   const int run = tid / A.E;
 
-  // Running receive spectrum of this thread, kept in shared memory ([j][thread]) so the
-  // registers go to the per-tile partials and the recurrence state.
-  float2* Ys = reinterpret_cast<float2*>(sm + L.off_y);
-#pragma unroll
-  for (int j = 0; j < kAnchor; ++j) Ys[j * kThreads + tid] = make_float2(0.f, 0.f);
-
   float* b_rhi = reinterpret_cast<float*>(sm + L.off_rhi);
   float* b_rlo = reinterpret_cast<float*>(sm + L.off_rlo);
   float* b_amp = reinterpret_cast<float*>(sm + L.off_amp);
@@ -228,118 +224,143 @@ __global__ void __launch_bounds__(kThreads, 1) simus_band_kernel(const BandArgs 
   const float2* pp = reinterpret_cast<const float2*>(sm + L.off_pp);
   const float* b_dir = reinterpret_cast<const float*>(sm + L.off_dir);
   const float* kb = reinterpret_cast<const float*>(sm + L.off_kb);
-  __syncthreads();
+  // Running receive spectrum of this thread, kept in shared memory ([j][thread]) so the
+  // registers go to the per-tile partials and the recurrence state.
+  float2* Ys = reinterpret_cast<float2*>(sm + L.off_y);
 
-  const float2 k_run = A.t.kf[min(f_b0 + (rx_on ? run : 0) * kAnchor, A.F - 1)];
-  const float a_run = A.t.af[min(f_b0 + (rx_on ? run : 0) * kAnchor, A.F - 1)];
-
+  const int64_t units = (int64_t)A.n_bands * A.chunk_tiles;
+  const int64_t u_end = (int64_t)(blockIdx.x + 1) * units / A.grid;
+  const int64_t s_stop = min(A.n_pts, A.chunk_s0 + A.chunk_tiles * A.st);
   uint32_t phase = 0;
-  for (int64_t t0 = s_begin; t0 < s_end; t0 += A.st) {
-    // ---------------- geometry: TMA bulk copy of the tile's block ----------------
-    // The previous tile's reads of these arrays finished at the barrier that closed it; the
-    // proxy fence orders them before the asynchronous writes.  Thread 0 waits (bounded) and
-    // the barrier publishes the data and the outcome to the CTA.
-    if (tid == 0) {
-      const unsigned char* src = A.geo + ((t0 - A.chunk_s0) / A.st) * A.geo_bytes;
-      tc::fence_proxy_async_smem();
-      tc::mbar_arrive_expect_tx(&s_mbar, (uint32_t)A.geo_bytes);
-      for (size_t off = 0; off < A.geo_bytes; off += kBulkPiece)
-        tc::bulk_g2s(sm + off, src + off, (uint32_t)min(kBulkPiece, A.geo_bytes - off), &s_mbar);
-      if (!tc::mbar_wait_bounded(&s_mbar, phase, kBulkWaitTries)) s_fail = 1;
-    }
-    phase ^= 1u;
-    __syncthreads();
-    if (s_fail) break;
-    // ---------------- TX ----------------
-    {
-      int64_t s = t0 + sl;
-      bool valid = s < s_end;
-      int64_t si = valid ? s : t0;
-      float w = 0.f;
-      if (valid) {
-        double x = A.pts[2 * si], z = A.pts[2 * si + 1];
-        bool out = z < 0.0;
-        if (A.convex) out = out || (x * x + (z + A.apex) * (z + A.apex) <= A.radius2);
-        w = out ? 0.f : (float)A.rc[si];
-      }
-      SimusSink sink{W, pp, w, sl, A.fb};
-      tx_tile<GN, false, FFD>(A, L, sm, si, sl, g, sink);
-    }
-    __syncthreads();
-    // ---------------- RX ----------------
-    if (rx_on) {
-      float2 Yt[kAnchor];
+  for (int64_t u = (int64_t)blockIdx.x * units / A.grid; u < u_end;) {
+    const int band = (int)(u / A.chunk_tiles);
+    const int64_t t_lo = u - (int64_t)band * A.chunk_tiles;
+    const int64_t t_hi = min(A.chunk_tiles, t_lo + (u_end - u));
+    u += t_hi - t_lo;
+    const int slot = (int)blockIdx.x - cta_of_unit((int64_t)band * A.chunk_tiles, units, A.grid);
+    const int f_b0 = band * A.fb;
+    // the previous segment's readers of the tables finished at the barrier that closed its
+    // last tile
+    load_band_tables(A, L, sm, f_b0);
 #pragma unroll
-      for (int j = 0; j < kAnchor; ++j) Yt[j] = make_float2(0.f, 0.f);
+    for (int j = 0; j < kAnchor; ++j) Ys[j * kThreads + tid] = make_float2(0.f, 0.f);
+    __syncthreads();
+
+    const float2 k_run = A.t.kf[min(f_b0 + (rx_on ? run : 0) * kAnchor, A.F - 1)];
+    const float a_run = A.t.af[min(f_b0 + (rx_on ? run : 0) * kAnchor, A.F - 1)];
+
+    for (int64_t tile = t_lo; tile < t_hi; ++tile) {
+      const int64_t t0 = A.chunk_s0 + tile * A.st;
+      // ---------------- geometry: TMA bulk copy of the tile's block ----------------
+      // The previous tile's reads of these arrays finished at the barrier that closed it; the
+      // proxy fence orders them before the asynchronous writes.  Thread 0 waits (bounded) and
+      // the barrier publishes the data and the outcome to the CTA.
+      if (tid == 0) {
+        const unsigned char* src = A.geo + tile * A.geo_bytes;
+        tc::fence_proxy_async_smem();
+        tc::mbar_arrive_expect_tx(&s_mbar, (uint32_t)A.geo_bytes);
+        for (size_t off = 0; off < A.geo_bytes; off += kBulkPiece)
+          tc::bulk_g2s(sm + off, src + off, (uint32_t)min(kBulkPiece, A.geo_bytes - off), &s_mbar);
+        if (!tc::mbar_wait_bounded(&s_mbar, phase, kBulkWaitTries)) s_fail = 1;
+      }
+      phase ^= 1u;
+      __syncthreads();
+      if (s_fail) break;
+      // ---------------- TX ----------------
+      {
+        int64_t s = t0 + sl;
+        bool valid = s < s_stop;
+        int64_t si = valid ? s : t0;
+        float w = 0.f;
+        if (valid) {
+          double x = A.pts[2 * si], z = A.pts[2 * si + 1];
+          bool out = z < 0.0;
+          if (A.convex) out = out || (x * x + (z + A.apex) * (z + A.apex) <= A.radius2);
+          w = out ? 0.f : (float)A.rc[si];
+        }
+        SimusSink sink{W, pp, w, sl, A.fb};
+        tx_tile<GN, false, FFD>(A, L, sm, si, sl, g, sink);
+      }
+      __syncthreads();
+      // ---------------- RX ----------------
+      if (rx_on) {
+        float2 Yt[kAnchor];
+#pragma unroll
+        for (int j = 0; j < kAnchor; ++j) Yt[j] = make_float2(0.f, 0.f);
 #pragma unroll 1
-      // two scatterers per pass (st is even): independent recurrences give the scheduler two
-      // chains per sub-element to interleave; both accumulate into the same partial
-      for (int s = 0; s < A.st; s += 2) {
-        // the scatterers' fields over my run of frequencies: contiguous, read 2 per load
-        const float4* Wa = reinterpret_cast<const float4*>(W + s * A.fb + run * kAnchor);
-        const float4* Wb = reinterpret_cast<const float4*>(W + (s + 1) * A.fb + run * kAnchor);
-        float2 Ga[U], Sa[U], Gb[U], Sb[U];
-        float2 Dab[FFD ? U : 1];  // FFD: half_seg sin(theta) of (s, s + 1)
+        // two scatterers per pass (st is even): independent recurrences give the scheduler two
+        // chains per sub-element to interleave; both accumulate into the same partial
+        for (int s = 0; s < A.st; s += 2) {
+          // the scatterers' fields over my run of frequencies: contiguous, read 2 per load
+          const float4* Wa = reinterpret_cast<const float4*>(W + s * A.fb + run * kAnchor);
+          const float4* Wb = reinterpret_cast<const float4*>(W + (s + 1) * A.fb + run * kAnchor);
+          float2 Ga[U], Sa[U], Gb[U], Sb[U];
+          float2 Dab[FFD ? U : 1];  // FFD: half_seg sin(theta) of (s, s + 1)
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int idx = u * L.plane + e_rx * L.pitch + s;
-          Ga[u] = anchor_value(b_rhi[idx], b_rlo[idx], b_amp[idx], k_run, a_run);
-          Sa[u] = b_st[idx];
-          Gb[u] = anchor_value(b_rhi[idx + 1], b_rlo[idx + 1], b_amp[idx + 1], k_run, a_run);
-          Sb[u] = b_st[idx + 1];
-          if constexpr (FFD) Dab[u] = make_float2(b_dir[idx], b_dir[idx + 1]);
-        }
-#pragma unroll
-        for (int j = 0; j < kAnchor; ++j) {
-          float2 ra, rb;
-          if constexpr (FFD) {
-            // each sub-element term weighted by its directivity at this frequency
-            const float k = kb[run * kAnchor + j];
-            ra = rb = make_float2(0.f, 0.f);
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-              const float2 d = sinc_poly2(__fmul2_rn(Dab[u], make_float2(k, k)));
-              ra = make_float2(fmaf(Ga[u].x, d.x, ra.x), fmaf(Ga[u].y, d.x, ra.y));
-              rb = make_float2(fmaf(Gb[u].x, d.y, rb.x), fmaf(Gb[u].y, d.y, rb.y));
-              Ga[u] = cmul(Ga[u], Sa[u]);
-              Gb[u] = cmul(Gb[u], Sb[u]);
-            }
-          } else {
-            ra = Ga[0];
-            rb = Gb[0];
-            Ga[0] = cmul(Ga[0], Sa[0]);
-            Gb[0] = cmul(Gb[0], Sb[0]);
-#pragma unroll
-            for (int u = 1; u < U; ++u) {
-              ra = cadd(ra, Ga[u]);
-              rb = cadd(rb, Gb[u]);
-              Ga[u] = cmul(Ga[u], Sa[u]);
-              Gb[u] = cmul(Gb[u], Sb[u]);
-            }
+          for (int u = 0; u < U; ++u) {
+            const int idx = u * L.plane + e_rx * L.pitch + s;
+            Ga[u] = anchor_value(b_rhi[idx], b_rlo[idx], b_amp[idx], k_run, a_run);
+            Sa[u] = b_st[idx];
+            Gb[u] = anchor_value(b_rhi[idx + 1], b_rlo[idx + 1], b_amp[idx + 1], k_run, a_run);
+            Sb[u] = b_st[idx + 1];
+            if constexpr (FFD) Dab[u] = make_float2(b_dir[idx], b_dir[idx + 1]);
           }
-          const float4 wa = Wa[j >> 1], wb = Wb[j >> 1];
-          Yt[j] = cfma((j & 1) ? make_float2(wa.z, wa.w) : make_float2(wa.x, wa.y), ra, Yt[j]);
-          Yt[j] = cfma((j & 1) ? make_float2(wb.z, wb.w) : make_float2(wb.x, wb.y), rb, Yt[j]);
+#pragma unroll
+          for (int j = 0; j < kAnchor; ++j) {
+            float2 ra, rb;
+            if constexpr (FFD) {
+              // each sub-element term weighted by its directivity at this frequency
+              const float k = kb[run * kAnchor + j];
+              ra = rb = make_float2(0.f, 0.f);
+#pragma unroll
+              for (int u = 0; u < U; ++u) {
+                const float2 d = sinc_poly2(__fmul2_rn(Dab[u], make_float2(k, k)));
+                ra = make_float2(fmaf(Ga[u].x, d.x, ra.x), fmaf(Ga[u].y, d.x, ra.y));
+                rb = make_float2(fmaf(Gb[u].x, d.y, rb.x), fmaf(Gb[u].y, d.y, rb.y));
+                Ga[u] = cmul(Ga[u], Sa[u]);
+                Gb[u] = cmul(Gb[u], Sb[u]);
+              }
+            } else {
+              ra = Ga[0];
+              rb = Gb[0];
+              Ga[0] = cmul(Ga[0], Sa[0]);
+              Gb[0] = cmul(Gb[0], Sb[0]);
+#pragma unroll
+              for (int u = 1; u < U; ++u) {
+                ra = cadd(ra, Ga[u]);
+                rb = cadd(rb, Gb[u]);
+                Ga[u] = cmul(Ga[u], Sa[u]);
+                Gb[u] = cmul(Gb[u], Sb[u]);
+              }
+            }
+            const float4 wa = Wa[j >> 1], wb = Wb[j >> 1];
+            Yt[j] = cfma((j & 1) ? make_float2(wa.z, wa.w) : make_float2(wa.x, wa.y), ra, Yt[j]);
+            Yt[j] = cfma((j & 1) ? make_float2(wb.z, wb.w) : make_float2(wb.x, wb.y), rb, Yt[j]);
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < kAnchor; ++j) Ys[j * kThreads + tid] = cadd(Ys[j * kThreads + tid], Yt[j]);
+      }
+      __syncthreads();
+    }
+    if (s_fail) break;
+    if (slot >= A.n_slots) {  // cannot happen for the host's slot count; fail loudly if it does
+      if (tid == 0) atomicExch(A.status, FSG_EINVAL);
+      break;
+    }
+    if (rx_on) {
+      float2* out = reinterpret_cast<float2*>(A.partial) + (size_t)slot * A.F * A.E;
+#pragma unroll
+      for (int j = 0; j < kAnchor; ++j) {
+        int f = f_b0 + run * kAnchor + j;
+        if (f < A.F) {
+          float2* o = out + (size_t)f * A.E + e_rx;
+          *o = cadd(*o, Ys[j * kThreads + tid]);
         }
       }
-#pragma unroll
-      for (int j = 0; j < kAnchor; ++j) Ys[j * kThreads + tid] = cadd(Ys[j * kThreads + tid], Yt[j]);
-    }
-    __syncthreads();
-  }
-  if (s_fail && tid == 0) atomicExch(A.status, FSG_ETIMEOUT);
-  if (rx_on) {
-    float2* out = reinterpret_cast<float2*>(A.partial) + (size_t)blockIdx.y * A.F * A.E;
-#pragma unroll
-    for (int j = 0; j < kAnchor; ++j) {
-      int f = f_b0 + run * kAnchor + j;
-      if (f < A.F) {
-        const float2 y = Ys[j * kThreads + tid];
-        float2* o = out + (size_t)f * A.E + e_rx;
-        *o = A.accumulate ? cadd(*o, y) : y;
-      }
     }
   }
+  if (tid == 0 && s_fail) atomicExch(A.status, FSG_ETIMEOUT);
 }
 
 struct PfieldSink {
@@ -392,7 +413,7 @@ static cudaError_t launch_simus_band(const SweepConfig& c, const BandArgs& A, cu
   cudaError_t e =
       cudaFuncSetAttribute(simus_band_kernel<U, GN, FFD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem);
   if (e != cudaSuccess) return e;
-  simus_band_kernel<U, GN, FFD><<<dim3(c.n_bands, c.n_slices), kThreads, c.smem, s>>>(A);
+  simus_band_kernel<U, GN, FFD><<<A.grid, kThreads, c.smem, s>>>(A);
   return cudaGetLastError();
 }
 
