@@ -260,11 +260,16 @@ SweepConfig pfield_config(int E, int U, int F, int64_t n_pts, int num_sms, int f
   c.gn = next_pow2((n_src + kSrcPerThread - 1) / kSrcPerThread);
   if (c.gn < 4) c.gn = 4;
   c.st = kThreads / c.gn;
-  int nb = (F + 127) / 128;
-  int per = (F + nb - 1) / nb;
+  const int64_t tiles = n_pts > 0 ? (n_pts + c.st - 1) / c.st : 1;
+  // Every band recomputes its points' geometry, so use as few bands as keep the two CTAs per
+  // SM busy with at least 8 tiles each (one band for large grids), and at most one band per
+  // kAnchor frequencies.
+  const int64_t want = (8 * 2 * (int64_t)num_sms + tiles - 1) / tiles;
+  const int max_nb = (F + kAnchor - 1) / kAnchor;
+  const int nb = want < 1 ? 1 : (want > max_nb ? max_nb : (int)want);
+  const int per = (F + nb - 1) / nb;
   c.fb = ((per + kAnchor - 1) / kAnchor) * kAnchor;
   c.n_bands = (F + c.fb - 1) / c.fb;
-  const int64_t tiles = n_pts > 0 ? (n_pts + c.st - 1) / c.st : 1;
   int64_t slices = (2 * (int64_t)num_sms) / c.n_bands;
   if (slices < 1) slices = 1;
   if (slices > tiles) slices = tiles;
