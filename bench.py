@@ -495,7 +495,8 @@ def other_paths(args) -> dict:
     out = {}
     for name, fn, kw in (("batched_fp32_cfg3", run_batched_workload, {"autotune_quick": True}),
                          ("tensor_core_cfg4", run_tc_workload, {}),
-                         ("surrogate_cfg5", run_surrogate_workload, {})):
+                         ("surrogate_cfg5", run_surrogate_workload, {}),
+                         ("beamform_das_cfg3", run_beamform_workload, {})):
         a = copy.copy(args)
         a.scatterers = 200_000  # each workload uses its own size
         a.steps, a.warmup = 3, 2
@@ -505,13 +506,116 @@ def other_paths(args) -> dict:
             r = fn(a)
             keep = ("metric", "value", "unit", "ms_per_step", "green_terms_per_s", "sweep_ms", "roofline", "paths",
                     "speedup_tc_vs_plain", "speedup_tc_vs_fp32_batched", "config", "training",
-                    "field_rel_l2_1M_queries", "per_query_s", "simus_1M_x75", "clocks")
+                    "field_rel_l2_1M_queries", "per_query_s", "simus_1M_x75", "clocks", "rf2iq_ms", "das_ms",
+                    "das_terms_per_s", "cpu_baseline", "parity_rel_l2_sample")
             out[name] = {k: r[k] for k in keep if k in r}
             if "training" in out[name]:
                 out[name]["training"] = {k: v for k, v in out[name]["training"].items() if k != "history"}
         except Exception as exc:  # recorded in the JSON line
             out[name] = {"error": f"{type(exc).__name__}: {exc}"}
     return out
+
+
+def run_beamform_workload(args):
+    """Imaging of the cfg3 firings downstream of simus: one seeded phantom of the cfg3 set
+    simulated for 75 plane waves at +-16 deg by the batched sweep, then rf2iq of the 75 RF
+    frames and the compounded delay-and-sum of all firings on a 256 x 512 grid of the cfg3 box
+    (x in [-10, 10] mm, z in [5, 30] mm), linear interpolation, default f-number.  A step is
+    rf2iq + das on HBM-resident RF (kernels timed with CUDA events on the launching stream).
+    The CPU baseline runs the FP64 oracle on a bounded sample (2 firings x 4,096 pixels),
+    scaled to the full image; the same sample gives the parity figure."""
+    import ctypes
+
+    import torch
+
+    from fastsimus_gb300 import _device, _native, build
+    from fastsimus_gb300 import workloads as W
+    from fastsimus_gb300.batched import BatchedSimus
+    from fastsimus_gb300.beamform import RF2IQ_ORDER, DasParam, _das_call, _lowpass, _pixels, das, rf2iq
+
+    build.build()
+    device = torch.device("cuda", _env_int("LOCAL_RANK", 0))
+    torch.cuda.set_device(device)
+    p, m = W.cfg1_probe(), W.cfg1_medium()
+    angles = np.linspace(-16.0, 16.0, getattr(args, "transmits", 75))
+    delays = np.asarray(W.plane_wave_delays(p, m, angles), dtype=np.float64)
+    b = BatchedSimus(W.cfg3_phantoms(1), delays, p, m)
+    b.run()
+    rf = b.rfs[0]  # (n_tx, n_samples, E) float32, HBM-resident
+    plan = b.plans[0]
+    fs = plan.n_fft * float(plan.selected_freqs[1] - plan.selected_freqs[0])  # exact RF sample rate
+    nt, ns, ne = rf.shape
+    xs, zs = np.linspace(-10e-3, 10e-3, 256), np.linspace(5e-3, 30e-3, 512)
+    x, z = np.meshgrid(xs, zs)
+    param = DasParam.from_params(p, m, fs=fs)
+    lib = _native.load()
+    stream = _device.stream_handle(device)
+    sos, zq = _lowpass(fs, p.freq_center, None)
+    dp = ctypes.POINTER(ctypes.c_double)
+    iq = torch.empty((nt, ne, ns), dtype=torch.complex64, device=device)
+    img = torch.empty(x.size, dtype=torch.complex64, device=device)
+    pix, _ = _pixels(x, z, device)
+    txd = torch.as_tensor(delays, device=device)
+    probe, dpar = _das_call(param, "linear", True)
+
+    def step(ev=None):
+        if ev:
+            ev[0].record()
+        _native.check(lib.fsg_rf2iq(rf.data_ptr(), nt, ns, ne, fs, p.freq_center, 0.0, sos.shape[0],
+                                    sos.ctypes.data_as(dp), zq.ctypes.data_as(dp), 3 * (RF2IQ_ORDER + 1),
+                                    iq.data_ptr(), stream))
+        if ev:
+            ev[1].record()
+        _native.check(lib.fsg_das(ctypes.byref(probe), ctypes.byref(dpar), iq.data_ptr(), nt, ns, txd.data_ptr(),
+                                  pix.data_ptr(), pix.shape[0], img.data_ptr(), stream))
+        if ev:
+            ev[2].record()
+
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    t_iq, t_das = [], []
+    with ClockSampler(device.index or 0) as clocks:
+        for _ in range(max(args.steps, 3)):
+            flush.zero_()
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            step(ev)
+            torch.cuda.synchronize()
+            t_iq.append(ev[0].elapsed_time(ev[1]))
+            t_das.append(ev[1].elapsed_time(ev[2]))
+    iq_ms, das_ms = float(np.median(t_iq)), float(np.median(t_das))
+    terms = x.size * nt * ne
+    # CPU oracle on a bounded sample, and the GPU image of the same sample for parity
+    from oracle import das_fp64 as D
+
+    rng = np.random.default_rng(0)
+    sel = rng.choice(x.size, 4096, replace=False)
+    fr = [0, nt - 1]
+    px, pz = x.reshape(-1)[sel], z.reshape(-1)[sel]
+    rf_h = rf[fr].cpu().numpy().astype(np.float64)
+    t0 = time.perf_counter()
+    iq_h = np.stack([D.rf2iq(rf_h[k], fs, p.freq_center) for k in range(len(fr))])
+    ref = D.das(iq_h, px, pz, delays[fr], n_elements=ne, pitch=p.pitch, radius=p.radius, c=m.speed_of_sound, fs=fs,
+                fc=p.freq_center, fnumber=D.default_fnumber(p.element_width, p.freq_center, m.speed_of_sound))
+    t_cpu = time.perf_counter() - t0
+    got = das(rf2iq(rf[fr], fs, p.freq_center), px, pz, delays[fr], param).cpu().numpy()
+    parity = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+    cpu_image_s = t_cpu * (x.size / sel.size) * (nt / len(fr))
+    return {
+        "metric": "compounded images/s (rf2iq + delay-and-sum of 75 plane-wave firings, 256 x 512 pixels)",
+        "value": 1e3 / (iq_ms + das_ms), "unit": "images/s", "ms_per_step": iq_ms + das_ms,
+        "rf2iq_ms": iq_ms, "das_ms": das_ms, "das_terms_per_s": terms / (das_ms * 1e-3),
+        "config": {"workload": "cfg3 probe (64 elements), one cfg3 phantom, 75 plane waves +-16 deg, "
+                               "256 x 512 grid over x [-10, 10] mm, z [5, 30] mm",
+                   "n_samples": ns, "fs_hz": fs, "fnumber": D.default_fnumber(p.element_width, p.freq_center,
+                                                                               m.speed_of_sound),
+                   "l2": "flushed (512 MiB write) before every step"},
+        "cpu_baseline": {"value": 1.0 / cpu_image_s, "unit": "images/s", "cores": 1, "kind": "port",
+                         "sample": f"2 firings x {sel.size} pixels, scaled x{x.size * nt / (sel.size * len(fr)):.0f}"},
+        "parity_rel_l2_sample": parity,
+        "clocks": clocks.summary(),
+    }
 
 
 def run_batched_workload(args):
@@ -834,9 +938,10 @@ def main():
     ap.add_argument("--scatterers", type=int, default=200_000, help="smaller values make profiling cases")
     ap.add_argument("--grid-nx", type=int, default=256)
     ap.add_argument("--grid-nz", type=int, default=512)
-    ap.add_argument("--workload", choices=["cfg2", "cfg3", "cfg4", "cfg5"], default="cfg2",
+    ap.add_argument("--workload", choices=["cfg2", "cfg3", "cfg4", "cfg5", "das"], default="cfg2",
                     help="cfg2: plain simus + pfield frame (default); cfg3: batched 75 waves x 16 phantoms; "
-                         "cfg4: tensor-core path vs FP32 paths, 31 waves x 262,144 scatterers")
+                         "cfg4: tensor-core path vs FP32 paths, 31 waves x 262,144 scatterers; cfg5: surrogate; "
+                         "das: rf2iq + delay-and-sum of 75 cfg3 firings")
     ap.add_argument("--tc-oracle-scatterers", type=int, default=16384)
     ap.add_argument("--tc-only", action="store_true", help="cfg4 profiling case: only the tensor-core sweep")
     ap.add_argument("--sur-train", type=int, default=2_000_000)
@@ -854,6 +959,8 @@ def main():
         print(json.dumps(run_tc_workload(args)), flush=True)
     elif args.workload == "cfg5":
         print(json.dumps(run_surrogate_workload(args)), flush=True)
+    elif args.workload == "das":
+        print(json.dumps(run_beamform_workload(args)), flush=True)
     else:
         run_gpu_arm(args, rank, world)
 

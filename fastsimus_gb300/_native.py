@@ -60,7 +60,17 @@ class FsgBatchTuning(ctypes.Structure):
                 ("ctas_per_sm", ctypes.c_int32), ("reserved0", ctypes.c_int32)]
 
 
+FSG_DAS_LINEAR, FSG_DAS_NEAREST = range(2)
+
+
+class FsgDasParams(ctypes.Structure):
+    _fields_ = [("speed_of_sound", ctypes.c_double), ("fs", ctypes.c_double), ("fc", ctypes.c_double),
+                ("t0", ctypes.c_double), ("fnumber", ctypes.c_double), ("method", ctypes.c_int32),
+                ("iq", ctypes.c_int32)]
+
+
 _P = ctypes.c_void_p
+_DP = ctypes.POINTER(ctypes.c_double)
 _SIGNATURES = {
     "fsg_abi_version": (ctypes.c_int32, []),
     "fsg_last_error_string": (ctypes.c_char_p, []),
@@ -114,6 +124,14 @@ _SIGNATURES = {
     "fsg_irfft_gate": (ctypes.c_int32, [_P, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
                                         ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P,
                                         ctypes.c_size_t, _P]),
+    "fsg_rf2iq": (ctypes.c_int32, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_double, ctypes.c_int32, _DP, _DP, ctypes.c_int32, _P,
+                                   _P]),
+    "fsg_das": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgDasParams), _P, ctypes.c_int32,
+                                 ctypes.c_int32, _P, _P, ctypes.c_int64, _P, _P]),
+    "fsg_dasmtx_nnz_per_row": (ctypes.c_int32, [ctypes.c_int32, ctypes.c_int32]),
+    "fsg_dasmtx": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgDasParams), ctypes.c_int32, _P, _P,
+                                    ctypes.c_int64, _P, _P, _P, _P]),
 }
 
 _lib = None

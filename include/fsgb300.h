@@ -292,6 +292,71 @@ int32_t fsg_irfft_gate(const void* spectrum, int32_t n_batch, int64_t batch_stri
                        int32_t n_elements, int32_t n_fft, int32_t k_first, int32_t k_count, int32_t gate,
                        float* rf_out, void* workspace, size_t workspace_bytes, void* stream);
 
+/*
+ * Downstream beamforming of the simulated RF.  The reference's validation tests image the RF
+ * with PyMUST (tests/_picmus_phantom_shared.py:407-460): pymust.rf2iq(rf, fs, fc), then
+ * pymust.dasmtx(1j * iq.shape, x, z, param) times the IQ flattened in Fortran order, summed over
+ * firings.  These entry points restate MUST's rf2iq / dasmtx algorithms on the GPU.
+ *
+ * fsg_rf2iq: I/Q demodulation.  Per column (frame, channel): x[n] = rf[n] exp(-2 pi i fc (n / fs
+ * + tau)); then a low-pass IIR filter run forward and backward (zero phase) over x extended at
+ * both ends by `pad` odd-reflected samples, each pass started from the filter's steady state for
+ * its first input; the result times 2.  (MUST: 5th-order Butterworth, Wn = min(2 fc / fs, 0.5),
+ * pad = 3 (order + 1), as scipy.signal.filtfilt.)  The filter is given as n_sections cascaded
+ * second-order sections sos[s] = (b0, b1, b2, 1, a1, a2) with steady-state states zi[s] = (z0, z1)
+ * for a unit input (scipy.signal.butter(..., output="sos"), scipy.signal.sosfilt_zi): the same
+ * transfer function as the (b, a) form, but well conditioned in FP32.  sos and zi are HOST arrays.
+ * rf: float32 [n_frames][n_samples][n_channels]; iq_out: complex64 [n_frames][n_channels][n_samples]
+ * (channel-major: the Fortran-order columns of each frame's (n_samples, n_channels) IQ).
+ * Requires 1 <= n_sections <= FSG_RF2IQ_MAX_SECTIONS and 0 <= pad < n_samples, pad <= FSG_RF2IQ_MAX_PAD.
+ */
+#define FSG_RF2IQ_MAX_SECTIONS 4
+#define FSG_RF2IQ_MAX_PAD 27
+int32_t fsg_rf2iq(const float* rf, int32_t n_frames, int32_t n_samples, int32_t n_channels, double fs, double fc,
+                  double tau, int32_t n_sections, const double* sos, const double* zi, int32_t pad, void* iq_out,
+                  void* stream);
+
+typedef enum FsgDasMethod { FSG_DAS_LINEAR = 0, FSG_DAS_NEAREST = 1 } FsgDasMethod;
+
+/* Delay-and-sum parameters (the fields of MUST's param that dasmtx reads besides the array). */
+typedef struct FsgDasParams {
+  double speed_of_sound;  /* c, m/s */
+  double fs;              /* sampling frequency of the signals, Hz */
+  double fc;              /* I/Q rotation frequency, Hz (0 for RF signals) */
+  double t0;              /* time of sample 0, s */
+  double fnumber;         /* receive f-number; <= 0: every element */
+  int32_t method;         /* FsgDasMethod */
+  int32_t iq;             /* 1: signals are I/Q (rotate by exp(2 pi i fc t)) */
+} FsgDasParams;
+
+/*
+ * fsg_das: matrix-free compounded delay-and-sum.  For pixel p and firing f,
+ *   d_tx = min over firing elements e of (c tx_delays[f][e] + |p - x_e|)   (NaN delay: not firing)
+ *   t_e  = (d_tx + |p - x_e|) / c,  s = (t_e - t0) fs  (fractional 0-based sample)
+ *   image[p] += sum over aperture elements e of interp(iq[f][e], s) * exp(2 pi i fc t_e)
+ * with linear interpolation between floor(s) and floor(s) + 1 (both inside the record) or the
+ * nearest sample; the receive aperture is |lateral| <= axial / (2 fnumber) in the element's frame.
+ * Element centres follow the probe (linear: (e - (E - 1) / 2) pitch; convex: radius).
+ * iq: complex64 [n_frames][n_elements][n_samples]; tx_delays: float64 [n_frames][n_elements];
+ * pixels: float64 [n_pixels][2] (x, z); image_out: complex64 [n_pixels] (overwritten).
+ */
+int32_t fsg_das(const FsgProbe* probe, const FsgDasParams* params, const void* iq, int32_t n_frames,
+                int32_t n_samples, const double* tx_delays, const double* pixels, int64_t n_pixels, void* image_out,
+                void* stream);
+
+/* Non-zeros per row of the fsg_dasmtx matrix: 2 n_elements (linear) or n_elements (nearest). */
+int32_t fsg_dasmtx_nnz_per_row(int32_t method, int32_t n_elements);
+
+/*
+ * fsg_dasmtx: the same delay-and-sum for one firing as a CSR matrix of n_pixels rows and
+ * n_samples * n_elements columns (column e * n_samples + i = sample i of element e), the
+ * matrix pymust.dasmtx returns.  Every row holds fsg_dasmtx_nnz_per_row entries in increasing
+ * column order; entries of elements outside the aperture or the record are explicit zeros.
+ * crow: int32 [n_pixels + 1]; col: int32 [n_pixels * nnz_per_row]; val: complex64 (same count).
+ */
+int32_t fsg_dasmtx(const FsgProbe* probe, const FsgDasParams* params, int32_t n_samples, const double* tx_delays,
+                   const double* pixels, int64_t n_pixels, int32_t* crow, int32_t* col, void* val, void* stream);
+
 /* Measurement utility, no counterpart in the reference: launches `blocks` x 256 threads of
  * independent FP32 FMA chains (`iters` iterations) and reports the FLOPs it performs, so a
  * caller can time it with events and state the device's FP32 FMA roofline.  `out` must hold

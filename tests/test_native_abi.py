@@ -50,3 +50,5 @@ def test_struct_layouts_match_header():
     assert ctypes.sizeof(_native.FsgFreqPlan) == 64
     assert ctypes.sizeof(_native.FsgMlpWeights) == 11 * 8
     assert _native.FsgFreqPlan.pulse_spectrum.offset == 48
+    assert ctypes.sizeof(_native.FsgDasParams) == 48
+    assert _native.FsgDasParams.method.offset == 40
