@@ -11,10 +11,10 @@
 // cut-offs; the cascade stays at ~1e-6); the down-mixing phase n fc / fs + fc tau is reduced to
 // [0, 1) cycles in FP64 before sincospif.
 //
-// das_kernel: one thread per pixel, looping over firings and elements.  The per-firing
-// transmit delays (times c) and the element frames sit in shared memory; the I/Q samples are
-// read channel-major, so the threads of a warp (consecutive pixels down an image column) read
-// nearby samples of the same element.
+// das_kernel: one thread per pixel, looping over groups of firings and, per element, over the
+// group's firings.  The transmit delays (times c) and the element frames sit in shared memory;
+// the I/Q samples are read channel-major, so the threads of a warp (consecutive pixels down an
+// image column) read nearby samples of the same element.
 
 #include <cuda_runtime.h>
 #include <math.h>
@@ -27,6 +27,7 @@ namespace fsg {
 
 constexpr int kDasThreads = 256;
 constexpr int kDasMaxE = 256;
+constexpr int kDasFrameGroup = 32;  // firings whose transmit distances a thread holds at a time
 
 struct Rf2IqArgs {
   const float* rf;   // [n_frames][n_samples][n_ch]
@@ -38,14 +39,19 @@ struct Rf2IqArgs {
   float zi[FSG_RF2IQ_MAX_SECTIONS][2];   // steady state for a unit input
 };
 
-// Down-mixed sample n of a column: rf[n] exp(-2 pi i (n fc / fs + fc tau)).
-__device__ __forceinline__ float2 downmix(const Rf2IqArgs& A, const float* col, int n) {
+constexpr int kIqChunk = 16;  // samples loaded ahead of the recurrence (memory-level parallelism)
+
+// Down-mixed value v of sample n: v exp(-2 pi i (n fc / fs + fc tau)).
+__device__ __forceinline__ float2 mix(const Rf2IqArgs& A, int n, float v) {
   const double cyc = fma((double)n, A.cyc_per_sample, A.cyc0);
   const float frac = (float)(cyc - floor(cyc));
   float s, c;
   sincospif(2.0f * frac, &s, &c);
-  const float v = col[(size_t)n * A.n_ch];
   return make_float2(v * c, -v * s);
+}
+
+__device__ __forceinline__ float2 downmix(const Rf2IqArgs& A, const float* col, int n) {
+  return mix(A, n, col[(size_t)n * A.n_ch]);
 }
 
 // One sample through the cascade of transposed direct-form-II biquads (real coefficients).
@@ -75,8 +81,8 @@ __global__ void __launch_bounds__(128) rf2iq_kernel(const __grid_constant__ Rf2I
   const int64_t colid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (colid >= (int64_t)A.n_frames * A.n_ch) return;
   const int fr = (int)(colid / A.n_ch), ch = (int)(colid % A.n_ch);
-  const float* col = A.rf + (size_t)fr * A.n_samples * A.n_ch + ch;
-  float2* y = A.iq + (size_t)colid * A.n_samples;
+  const float* __restrict__ col = A.rf + (size_t)fr * A.n_samples * A.n_ch + ch;
+  float2* __restrict__ y = A.iq + (size_t)colid * A.n_samples;
   const int N = A.n_samples, P = A.pad;
   float2 z[NS][2];
   float2 right[FSG_RF2IQ_MAX_PAD];
@@ -90,7 +96,15 @@ __global__ void __launch_bounds__(128) rf2iq_kernel(const __grid_constant__ Rf2I
     const float2 v = downmix(A, col, P - k);
     iir_step<NS>(A, z, make_float2(2.f * x0.x - v.x, 2.f * x0.y - v.y));
   }
-  for (int n = 0; n < N; ++n) y[n] = iir_step<NS>(A, z, downmix(A, col, n));
+  // the recurrence is sequential, the loads are not: each chunk's samples are requested first
+  for (int n0 = 0; n0 < N; n0 += kIqChunk) {
+    float v[kIqChunk];
+#pragma unroll
+    for (int j = 0; j < kIqChunk; ++j) v[j] = n0 + j < N ? col[(size_t)(n0 + j) * A.n_ch] : 0.f;
+#pragma unroll
+    for (int j = 0; j < kIqChunk; ++j)
+      if (n0 + j < N) y[n0 + j] = iir_step<NS>(A, z, mix(A, n0 + j, v[j]));
+  }
   for (int k = 0; k < P; ++k) {
     const float2 v = downmix(A, col, N - 2 - k);
     right[k] = iir_step<NS>(A, z, make_float2(2.f * xn.x - v.x, 2.f * xn.y - v.y));
@@ -98,9 +112,16 @@ __global__ void __launch_bounds__(128) rf2iq_kernel(const __grid_constant__ Rf2I
   // backward pass, started from the last forward output
   iir_init<NS>(A, z, P > 0 ? right[P - 1] : y[N - 1]);
   for (int k = P - 1; k >= 0; --k) iir_step<NS>(A, z, right[k]);
-  for (int n = N - 1; n >= 0; --n) {
-    const float2 o = iir_step<NS>(A, z, y[n]);
-    y[n] = make_float2(2.f * o.x, 2.f * o.y);
+  for (int n1 = N - 1; n1 >= 0; n1 -= kIqChunk) {
+    float2 w[kIqChunk];
+#pragma unroll
+    for (int j = 0; j < kIqChunk; ++j) w[j] = n1 - j >= 0 ? y[n1 - j] : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < kIqChunk; ++j)
+      if (n1 - j >= 0) {
+        const float2 o = iir_step<NS>(A, z, w[j]);
+        y[n1 - j] = make_float2(2.f * o.x, 2.f * o.y);
+      }
   }
 }
 
@@ -186,41 +207,77 @@ __device__ __forceinline__ bool das_tap(const DasArgs& A, const DasShared& S, in
   return true;
 }
 
-__global__ void __launch_bounds__(kDasThreads) das_kernel(const __grid_constant__ DasArgs A) {
+// Matrix-free compounded delay-and-sum.  The I/Q rotation exp(2 pi i fc (d_tx + d_rx) / c)
+// factors into a transmit part per (pixel, firing) and a receive part per (pixel, element), so
+// a thread first computes, for a group of firings, the transmit distance and rotation (kept in
+// registers / local memory), then per element the receive distance, aperture test and rotation
+// once, and per firing only the sample gather, the interpolation and one complex multiply-add.
+// The group's transmit delays (times c) sit in dynamic shared memory, [firing][element].
+__global__ void __launch_bounds__(kDasThreads) das_kernel(const __grid_constant__ DasArgs A, int group) {
   __shared__ DasShared S;
+  extern __shared__ float ctx_g[];  // [group][E]
   das_load_elements(A, S);
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = p < A.n_pix;
   const float px = valid ? (float)A.pix[2 * p] : 0.f, pz = valid ? (float)A.pix[2 * p + 1] : 0.f;
+  const float k_cyc = 0.5f * A.two_fc * A.inv_c;  // cycles per metre of path, fc / c
+  float dtx[kDasFrameGroup];
+  float2 rtx[kDasFrameGroup];
   float2 acc = make_float2(0.f, 0.f);
-  for (int f = 0; f < A.n_frames; ++f) {
+  for (int g0 = 0; g0 < A.n_frames; g0 += group) {
+    const int ng = min(group, A.n_frames - g0);
     __syncthreads();
-    das_load_delays(A, S, f);
+    for (int i = threadIdx.x; i < ng * A.E; i += blockDim.x) {
+      const double v = A.txd[(size_t)g0 * A.E + i];
+      ctx_g[i] = isnan(v) ? INFINITY : (float)(A.c * v);
+    }
     __syncthreads();
     if (!valid) continue;
-    const float dtx = das_dtx(A, S, px, pz);
-    if (!(dtx < INFINITY)) continue;
-    const float2* fr = A.iq + (size_t)f * A.E * A.n_s;
-    for (int e = 0; e < A.E; ++e) {
-      float s;
-      float2 rot;
-      if (!das_tap(A, S, e, px, pz, dtx, &s, &rot)) continue;
-      const float2* ce = fr + (size_t)e * A.n_s;
-      float2 v;
-      if (A.method == FSG_DAS_LINEAR) {
-        const float fi = floorf(s);
-        if (!(fi >= 0.f) || !(fi + 1.f <= (float)(A.n_s - 1))) continue;
-        const int i0 = (int)fi;
-        const float w = s - fi;
-        const float2 a = ce[i0], b = ce[i0 + 1];
-        v = make_float2(fmaf(w, b.x - a.x, a.x), fmaf(w, b.y - a.y, a.y));
-      } else {
-        const float fi = floorf(s + 0.5f);
-        if (!(fi >= 0.f) || !(fi <= (float)(A.n_s - 1))) continue;
-        v = ce[(int)fi];
+    for (int j = 0; j < ng; ++j) {
+      const float* cj = ctx_g + j * A.E;
+      float d = INFINITY;
+      for (int e = 0; e < A.E; ++e) {
+        const float dx = px - S.ex[e], dz = pz - S.ez[e];
+        d = fminf(d, cj[e] + sqrtf(fmaf(dx, dx, dz * dz)));
       }
-      acc.x += v.x * rot.x - v.y * rot.y;
-      acc.y += v.x * rot.y + v.y * rot.x;
+      dtx[j] = d;
+      float sn = 0.f, cs = 1.f;
+      if (A.iq_rot && d < INFINITY) sincospif(2.f * k_cyc * d, &sn, &cs);
+      rtx[j] = make_float2(cs, sn);
+    }
+    for (int e = 0; e < A.E; ++e) {
+      const float dx = px - S.ex[e], dz = pz - S.ez[e];
+      if (A.aperture >= 0.f) {
+        const float ax = fmaf(dx, S.es[e], dz * S.ec[e]);
+        const float lat = fmaf(dx, S.ec[e], -dz * S.es[e]);
+        if (!(ax > 0.f) || fabsf(lat) > ax * A.aperture) continue;
+      }
+      const float dr = sqrtf(fmaf(dx, dx, dz * dz));
+      float2 ae = make_float2(0.f, 0.f);
+      const float2* ce = A.iq + ((size_t)g0 * A.E + e) * A.n_s;
+      for (int j = 0; j < ng; ++j, ce += (size_t)A.E * A.n_s) {
+        const float t = (dtx[j] + dr) * A.inv_c;
+        const float s = (t - A.t0) * A.fs;
+        float2 v;
+        if (A.method == FSG_DAS_LINEAR) {
+          const float fi = floorf(s);
+          if (!(fi >= 0.f) || !(fi + 1.f <= (float)(A.n_s - 1))) continue;
+          const int i0 = (int)fi;
+          const float w = s - fi;
+          const float2 a = ce[i0], b = ce[i0 + 1];
+          v = make_float2(fmaf(w, b.x - a.x, a.x), fmaf(w, b.y - a.y, a.y));
+        } else {
+          const float fi = floorf(s + 0.5f);
+          if (!(fi >= 0.f) || !(fi <= (float)(A.n_s - 1))) continue;
+          v = ce[(int)fi];
+        }
+        ae.x = fmaf(v.x, rtx[j].x, fmaf(-v.y, rtx[j].y, ae.x));
+        ae.y = fmaf(v.x, rtx[j].y, fmaf(v.y, rtx[j].x, ae.y));
+      }
+      float sn = 0.f, cs = 1.f;
+      if (A.iq_rot) sincospif(2.f * k_cyc * dr, &sn, &cs);
+      acc.x = fmaf(ae.x, cs, fmaf(-ae.y, sn, acc.x));
+      acc.y = fmaf(ae.x, sn, fmaf(ae.y, cs, acc.y));
     }
   }
   if (valid) A.out[p] = acc;
@@ -351,8 +408,9 @@ extern "C" int32_t fsg_das(const FsgProbe* probe, const FsgDasParams* params, co
   if (n_pixels == 0) return FSG_OK;
   A.iq = static_cast<const float2*>(iq);
   A.out = static_cast<float2*>(image_out);
-  das_kernel<<<(unsigned)((n_pixels + kDasThreads - 1) / kDasThreads), kDasThreads, 0,
-               reinterpret_cast<cudaStream_t>(stream)>>>(A);
+  const int group = n_frames < kDasFrameGroup ? n_frames : kDasFrameGroup;
+  das_kernel<<<(unsigned)((n_pixels + kDasThreads - 1) / kDasThreads), kDasThreads,
+               (size_t)group * A.E * sizeof(float), reinterpret_cast<cudaStream_t>(stream)>>>(A, group);
   return check_cuda(cudaGetLastError(), "das_kernel launch");
 }
 
