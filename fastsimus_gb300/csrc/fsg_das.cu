@@ -8,8 +8,9 @@
 // (outputs of the record written to the channel-major IQ array, those of the right extension
 // kept in a local array), then backward over them in place.  The filter runs as cascaded
 // second-order sections in FP32 (a single high-order recursion loses ~1e-3 in FP32 at narrow
-// cut-offs; the cascade stays at ~1e-6); the down-mixing phase n fc / fs + fc tau is reduced to
-// [0, 1) cycles in FP64 before sincospif.
+// cut-offs; the cascade stays at ~1e-6).  The down-mixing phasors depend on the sample only:
+// each CTA tabulates them in shared memory (phase n fc / fs + fc tau reduced to [0, 1) cycles
+// in FP64, then sincospif), so a column's step is a load, a multiply and the biquads.
 //
 // das_kernel: one thread per pixel, looping over groups of firings and, per element, over the
 // group's firings.  The transmit delays (times c) and the element frames sit in shared memory;
@@ -25,7 +26,8 @@
 
 namespace fsg {
 
-constexpr int kDasThreads = 256;
+constexpr int kDasThreads = 256;      // dasmtx_kernel
+constexpr int kDasImgThreads = 128;   // das_kernel: small CTAs spread the pixels evenly over the SMs
 constexpr int kDasMaxE = 256;
 constexpr int kDasFrameGroup = 32;  // firings whose transmit distances a thread holds at a time
 
@@ -39,19 +41,24 @@ struct Rf2IqArgs {
   float zi[FSG_RF2IQ_MAX_SECTIONS][2];   // steady state for a unit input
 };
 
-constexpr int kIqChunk = 16;  // samples loaded ahead of the recurrence (memory-level parallelism)
+constexpr int kIqChunk = 16;     // samples loaded ahead of the recurrence (memory-level parallelism)
+constexpr int kIqTable = 2048;   // down-mixing phasors shared by a CTA's columns, per pass
+constexpr int kIqThreads = 64;
 
-// Down-mixed value v of sample n: v exp(-2 pi i (n fc / fs + fc tau)).
-__device__ __forceinline__ float2 mix(const Rf2IqArgs& A, int n, float v) {
+// Down-mixing phasor of sample n: exp(-2 pi i (n fc / fs + fc tau)), the phase reduced to
+// cycles in FP64.
+__device__ __forceinline__ float2 phasor(const Rf2IqArgs& A, int n) {
   const double cyc = fma((double)n, A.cyc_per_sample, A.cyc0);
   const float frac = (float)(cyc - floor(cyc));
   float s, c;
   sincospif(2.0f * frac, &s, &c);
-  return make_float2(v * c, -v * s);
+  return make_float2(c, -s);
 }
 
 __device__ __forceinline__ float2 downmix(const Rf2IqArgs& A, const float* col, int n) {
-  return mix(A, n, col[(size_t)n * A.n_ch]);
+  const float v = col[(size_t)n * A.n_ch];
+  const float2 e = phasor(A, n);
+  return make_float2(v * e.x, v * e.y);
 }
 
 // One sample through the cascade of transposed direct-form-II biquads (real coefficients).
@@ -77,34 +84,50 @@ __device__ __forceinline__ void iir_init(const Rf2IqArgs& A, float2 (*z)[2], flo
 }
 
 template <int NS>
-__global__ void __launch_bounds__(128) rf2iq_kernel(const __grid_constant__ Rf2IqArgs A) {
+__global__ void __launch_bounds__(kIqThreads) rf2iq_kernel(const __grid_constant__ Rf2IqArgs A) {
+  __shared__ float2 ph[kIqTable];  // phasors of the samples n0 .. n0 + kIqTable - 1
   const int64_t colid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (colid >= (int64_t)A.n_frames * A.n_ch) return;
-  const int fr = (int)(colid / A.n_ch), ch = (int)(colid % A.n_ch);
+  const bool active = colid < (int64_t)A.n_frames * A.n_ch;
+  const int64_t cid = active ? colid : 0;
+  const int fr = (int)(cid / A.n_ch), ch = (int)(cid % A.n_ch);
   const float* __restrict__ col = A.rf + (size_t)fr * A.n_samples * A.n_ch + ch;
-  float2* __restrict__ y = A.iq + (size_t)colid * A.n_samples;
+  float2* __restrict__ y = A.iq + (size_t)cid * A.n_samples;
   const int N = A.n_samples, P = A.pad;
   float2 z[NS][2];
   float2 right[FSG_RF2IQ_MAX_PAD];
-  const float2 x0 = downmix(A, col, 0), xn = downmix(A, col, N - 1);
+  float2 x0 = make_float2(0.f, 0.f), xn = x0;
   // forward pass over [2 x0 - x[P..1], x[0..N-1], 2 x[N-1] - x[N-2..N-1-P]]
-  {
+  if (active) {
+    x0 = downmix(A, col, 0);
+    xn = downmix(A, col, N - 1);
     const float2 xp = downmix(A, col, P);
     iir_init<NS>(A, z, P > 0 ? make_float2(2.f * x0.x - xp.x, 2.f * x0.y - xp.y) : x0);
+    for (int k = 0; k < P; ++k) {
+      const float2 v = downmix(A, col, P - k);
+      iir_step<NS>(A, z, make_float2(2.f * x0.x - v.x, 2.f * x0.y - v.y));
+    }
   }
-  for (int k = 0; k < P; ++k) {
-    const float2 v = downmix(A, col, P - k);
-    iir_step<NS>(A, z, make_float2(2.f * x0.x - v.x, 2.f * x0.y - v.y));
-  }
-  // the recurrence is sequential, the loads are not: each chunk's samples are requested first
-  for (int n0 = 0; n0 < N; n0 += kIqChunk) {
-    float v[kIqChunk];
+  // the record: the phasors are the same for every column, so the CTA tabulates them; the
+  // recurrence is sequential, the loads are not, so each chunk's samples are requested first
+  for (int n0 = 0; n0 < N; n0 += kIqTable) {
+    __syncthreads();
+    for (int j = threadIdx.x; j < kIqTable && n0 + j < N; j += blockDim.x) ph[j] = phasor(A, n0 + j);
+    __syncthreads();
+    if (!active) continue;
+    const int n_end = min(N, n0 + kIqTable);
+    for (int m0 = n0; m0 < n_end; m0 += kIqChunk) {
+      float v[kIqChunk];
 #pragma unroll
-    for (int j = 0; j < kIqChunk; ++j) v[j] = n0 + j < N ? col[(size_t)(n0 + j) * A.n_ch] : 0.f;
+      for (int j = 0; j < kIqChunk; ++j) v[j] = m0 + j < n_end ? col[(size_t)(m0 + j) * A.n_ch] : 0.f;
 #pragma unroll
-    for (int j = 0; j < kIqChunk; ++j)
-      if (n0 + j < N) y[n0 + j] = iir_step<NS>(A, z, mix(A, n0 + j, v[j]));
+      for (int j = 0; j < kIqChunk; ++j)
+        if (m0 + j < n_end) {
+          const float2 e = ph[m0 + j - n0];
+          y[m0 + j] = iir_step<NS>(A, z, make_float2(v[j] * e.x, v[j] * e.y));
+        }
+    }
   }
+  if (!active) return;
   for (int k = 0; k < P; ++k) {
     const float2 v = downmix(A, col, N - 2 - k);
     right[k] = iir_step<NS>(A, z, make_float2(2.f * xn.x - v.x, 2.f * xn.y - v.y));
@@ -213,7 +236,7 @@ __device__ __forceinline__ bool das_tap(const DasArgs& A, const DasShared& S, in
 // registers / local memory), then per element the receive distance, aperture test and rotation
 // once, and per firing only the sample gather, the interpolation and one complex multiply-add.
 // The group's transmit delays (times c) sit in dynamic shared memory, [firing][element].
-__global__ void __launch_bounds__(kDasThreads) das_kernel(const __grid_constant__ DasArgs A, int group) {
+__global__ void __launch_bounds__(kDasImgThreads) das_kernel(const __grid_constant__ DasArgs A, int group) {
   __shared__ DasShared S;
   extern __shared__ float ctx_g[];  // [group][E]
   das_load_elements(A, S);
@@ -354,13 +377,13 @@ extern "C" int32_t fsg_rf2iq(const float* rf, int32_t n_frames, int32_t n_sample
     for (int k = 0; k < 2; ++k) A.zi[sct][k] = on ? (float)zi[2 * sct + k] : 0.f;
   }
   const int64_t cols = (int64_t)n_frames * n_channels;
-  const unsigned grid = (unsigned)((cols + 127) / 128);
+  const unsigned grid = (unsigned)((cols + kIqThreads - 1) / kIqThreads);
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   switch (n_sections) {
-    case 1: rf2iq_kernel<1><<<grid, 128, 0, s>>>(A); break;
-    case 2: rf2iq_kernel<2><<<grid, 128, 0, s>>>(A); break;
-    case 3: rf2iq_kernel<3><<<grid, 128, 0, s>>>(A); break;
-    default: rf2iq_kernel<4><<<grid, 128, 0, s>>>(A); break;
+    case 1: rf2iq_kernel<1><<<grid, kIqThreads, 0, s>>>(A); break;
+    case 2: rf2iq_kernel<2><<<grid, kIqThreads, 0, s>>>(A); break;
+    case 3: rf2iq_kernel<3><<<grid, kIqThreads, 0, s>>>(A); break;
+    default: rf2iq_kernel<4><<<grid, kIqThreads, 0, s>>>(A); break;
   }
   return check_cuda(cudaGetLastError(), "rf2iq_kernel launch");
 }
@@ -409,7 +432,7 @@ extern "C" int32_t fsg_das(const FsgProbe* probe, const FsgDasParams* params, co
   A.iq = static_cast<const float2*>(iq);
   A.out = static_cast<float2*>(image_out);
   const int group = n_frames < kDasFrameGroup ? n_frames : kDasFrameGroup;
-  das_kernel<<<(unsigned)((n_pixels + kDasThreads - 1) / kDasThreads), kDasThreads,
+  das_kernel<<<(unsigned)((n_pixels + kDasImgThreads - 1) / kDasImgThreads), kDasImgThreads,
                (size_t)group * A.E * sizeof(float), reinterpret_cast<cudaStream_t>(stream)>>>(A, group);
   return check_cuda(cudaGetLastError(), "das_kernel launch");
 }
