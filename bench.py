@@ -135,6 +135,34 @@ def green_terms(plan, pplan, params, n_scat, n_grid):
     return n_scat * e_u * plan.selected_freqs.shape[0] + n_grid * e_u * pplan.selected_freqs.shape[0]
 
 
+def replica_throughput(local_ms: float, steps: int, dist=None, device="cpu"):
+    """Whole-job frames/s of independent replicas, one per rank: every rank ran `steps` frames
+    in `local_ms`; the job took as long as its slowest rank.  Returns (frames/s, job ms)."""
+    import torch
+
+    world, job_ms = 1, float(local_ms)
+    if dist is not None and dist.is_initialized():
+        world = dist.get_world_size()
+        t = torch.tensor([job_ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        job_ms = float(t.item())
+    return steps * world / (job_ms * 1e-3), job_ms
+
+
+def frame_launches(plan, params, n_scat, device) -> int:
+    """This library's kernel launches in one timed frame: fsg_simus (set-up, geometry + band
+    kernel per scatterer chunk, reduction), the RF epilogue (twiddles, irfft, gate) and
+    fsg_pfield (set-up, band kernel, reduction)."""
+    from fastsimus_gb300 import _device, _native
+
+    lib = _native.load()
+    fplan = _device.plan_tables(plan, device).fsg_plan(plan)
+    n = int(lib.fsg_simus_launches(_native.make_probe(params, plan.n_sub), fplan, int(n_scat), 0))
+    if n < 0:
+        raise RuntimeError("fsg_simus_launches rejected the frame")
+    return n + 3 + 3
+
+
 def algorithmic_flops_simus(plan, params, n_scat, n_tx=1):
     """S * F * (8 E U + 16 E T): recurrence (6) + sub-sum (2) per term, TX and RX complex MAC
     (8 + 8) per (scatterer, element, frequency, transmit)."""
@@ -322,13 +350,9 @@ def run_gpu_arm(args, rank, world):
         torch.cuda.synchronize()
         _device.set_timer(None)
     dev_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    value, dev_ms = replica_throughput(dev_ms, args.steps, dist, device)
     if dist is not None:
-        t = torch.tensor([dev_ms], device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_ms = float(t.item())
         dist.barrier()
-    frames = args.steps * world
-    value = frames / (dev_ms * 1e-3)
     simus_ms = timer.elapsed_ms("fsg_simus")
     pfield_ms = timer.elapsed_ms("fsg_pfield")
 
@@ -364,12 +388,7 @@ def run_gpu_arm(args, rank, world):
         torch.cuda.synchronize()
         if k >= args.warmup:
             e2e_ms.append(s.elapsed_time(e))
-    e2e_total = sum(e2e_ms)
-    if dist is not None:
-        t = torch.tensor([e2e_total], device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e_value = frames / (e2e_total * 1e-3)
+    e2e_value, _ = replica_throughput(sum(e2e_ms), args.steps, dist, device)
 
     if rank != 0:
         if dist is not None:
@@ -392,7 +411,7 @@ def run_gpu_arm(args, rank, world):
                    "n_sub": int(plan.n_sub), "plan_host_s": t_plan},
         "green_terms_per_s": gt * value,
         "simus_ms": simus_avg, "pfield_ms": float(np.mean(pfield_ms)) if pfield_ms else None,
-        "gpu_launches": 6 * args.steps,
+        "gpu_launches": args.steps * frame_launches(plan, params, n_scat, device),
         "roofline": {"kernel": "simus_band_kernel", "bound": "fp32", "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak if peak else None, "traffic": None,
                      "peak_source": "measured in-run by fsg_fp32_fma_probe (FP32 FMA chains); MEASURED_PEAKS.json "

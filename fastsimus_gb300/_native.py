@@ -76,6 +76,8 @@ _SIGNATURES = {
     "fsg_last_error_string": (ctypes.c_char_p, []),
     "fsg_simus_workspace_size": (ctypes.c_size_t, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgFreqPlan),
                                                    ctypes.c_int64]),
+    "fsg_simus_launches": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgFreqPlan), ctypes.c_int64,
+                                            ctypes.c_int32]),
     "fsg_simus": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgMedium), ctypes.POINTER(FsgFreqPlan),
                                    _P, _P, ctypes.c_int64, _P, _P, ctypes.c_int32, ctypes.c_int32, _P, _P,
                                    ctypes.c_size_t, _P]),

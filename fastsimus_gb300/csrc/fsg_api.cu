@@ -314,6 +314,14 @@ extern "C" size_t fsg_simus_workspace_size(const FsgProbe* probe, const FsgFreqP
   return simus_ws_size(probe, plan, n_scat, sms);
 }
 
+extern "C" int32_t fsg_simus_launches(const FsgProbe* probe, const FsgFreqPlan* plan, int64_t n_scat, int32_t ffd) {
+  if (!probe || !plan || probe->n_elements < 1 || probe->n_sub < 1 || plan->n_freq < 1 || n_scat < 0) return -1;
+  int sms = 0;
+  if (device_sm_count(&sms) != FSG_OK) return -1;
+  const SweepConfig c = simus_config(probe->n_elements, probe->n_sub, plan->n_freq, n_scat, sms, kGeoCacheBudget, ffd);
+  return 2 + (n_scat > 0 ? (int32_t)(2 * c.n_chunks) : 0);  // setup_tables, per chunk geometry + band, simus_reduce
+}
+
 extern "C" int32_t fsg_simus(const FsgProbe* probe, const FsgMedium* medium, const FsgFreqPlan* plan,
                              const double* scat_xz, const double* rc, int64_t n_scat, const double* delays,
                              const double* apod, int32_t ffd, int32_t out_layout, void* out, void* workspace,

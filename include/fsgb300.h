@@ -96,6 +96,11 @@ const char* fsg_last_error_string(void);
 /* Workspace bytes needed by fsg_simus for this probe / plan / scatterer count. */
 size_t fsg_simus_workspace_size(const FsgProbe* probe, const FsgFreqPlan* plan, int64_t n_scat);
 
+/* Kernel launches one fsg_simus call makes with the default workspace (set-up, a geometry and a
+ * band kernel per scatterer chunk, the reduction), or -1 for invalid arguments.  No counterpart
+ * in the reference: a measurement aid. */
+int32_t fsg_simus_launches(const FsgProbe* probe, const FsgFreqPlan* plan, int64_t n_scat, int32_t ffd);
+
 /*
  * Plain fused FP32 simus sweep for one transmit.
  * Replaces simus_cuda(scatterers, rc, params, plan, medium, delays_clean, tx_apodization)
