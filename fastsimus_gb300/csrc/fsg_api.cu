@@ -289,7 +289,7 @@ extern "C" int32_t fsg_abi_version(void) { return FSG_ABI_VERSION; }
 
 extern "C" const char* fsg_last_error_string(void) { return g_last_error.c_str(); }
 
-// Workspace: tables | status word | partial spectra [n_slices][F][E] | geometry cache.
+// Workspace: tables | status word | partial spectra [slots][F][E] | geometry cache.
 static size_t simus_ws_size(const SweepConfig& c, int E, int U, int F) {
   return tables_bytes(E, U, F) + 256 + align256((size_t)c.n_slices * F * E * 8) +
          align256((size_t)c.chunk_tiles * c.geo_bytes);

@@ -5,7 +5,7 @@
 // scanner's real-time processing chain, an inference-server backend with a fixed memory
 // budget), or code that must not synchronise the device mid-stream, which cudaMalloc/cudaFree
 // may do.  This entry point takes the same inputs and outputs as fsg_simus but no workspace:
-// its scratch (the per-frequency tables and the per-slice partial spectra) lives in the
+// its scratch (the per-frequency tables and the partial spectra) lives in the
 // file-scope device array below.
 //
 // Limits and behaviour:
@@ -19,8 +19,9 @@
 //     device, with that device current, asks the runtime for the address
 //     (cudaGetSymbolAddress) and caches it; make that first call before any stream capture.
 //   - All calls share the array and it keeps the last call's contents.  Every byte the sweep
-//     reads is written earlier in the same call (tables by the set-up kernel, partials by the
-//     band kernel, one entry per (slice, frequency, element)), so nothing has to start at zero.
+//     reads is written earlier in the same call (tables by the set-up kernel; the partial
+//     spectra are zeroed by the call, then accumulated by the band kernels), so nothing has to
+//     start at zero.
 //   - Calls whose work overlaps on the GPU (different streams, or different host threads on
 //     one device) race on the shared scratch and corrupt each other's results; serialise them.
 //   - The call allocates nothing: no cudaMalloc, no cudaFree, no allocating library routine.

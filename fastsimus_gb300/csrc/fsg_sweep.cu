@@ -7,13 +7,14 @@
 //                      (obliquity x centre-frequency sinc / sqrt(r) / n_sub), recurrence step
 //                      (and half_seg sin(theta) with full-frequency directivity), written as
 //                      one shared-memory-layout block per tile into an L2-sized cache;
-//   simus_band_kernel  grid (frequency band, slice of tiles); per tile: TMA bulk copy of the
-//                      tile's block, TX (packed FP32x2 recurrences, reduce-scatter of the
-//                      source sums across the point's lanes, W[s][f] = rc pulse probe P), RX
-//                      (thread = element x 32 frequencies, Y[e][f] += W[s][f] mean_u G);
-// then simus_reduce sums the slices' partial spectra in a fixed order.  Neither the
+//   simus_band_kernel  one CTA per SM, each sweeping an even share of the chunk's (band, tile)
+//                      units; per tile: TMA bulk copy of the tile's block, TX (packed FP32x2
+//                      recurrences, reduce-scatter of the source sums across the point's lanes,
+//                      W[s][f] = rc pulse probe P), RX (thread = element x 32 frequencies,
+//                      Y[e][f] += W[s][f] mean_u G), added into the band's partial slot;
+// then simus_reduce sums the slots' partial spectra in a fixed order.  Neither the
 // scatterer x element Green's tile nor W ever leaves the SM.
-// pfield: pfield_band_kernel computes its geometry in place (3 bands share little) and
+// pfield: pfield_band_kernel computes its geometry in place (one band for large grids) and
 // accumulates |pulse probe P|^2; pfield_reduce sums the bands and takes the square root.
 
 #include <cuda_runtime.h>
@@ -118,7 +119,7 @@ __global__ void __launch_bounds__(kThreads) geometry_kernel(const BandArgs A, in
   }
 }
 
-// out (layout) = probe_f * corr * sum over slices of partial[q][f][e], fixed slice order.
+// out (layout) = probe_f * corr * sum over slots of partial[q][f][e], fixed slot order.
 __global__ void simus_reduce(const float2* __restrict__ partial, int n_slices, int F, int E,
                              const float* __restrict__ probe, float corr, int full, int n_rows, int idx0,
                              const int* __restrict__ status, float2* __restrict__ out) {
