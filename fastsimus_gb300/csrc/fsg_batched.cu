@@ -278,6 +278,7 @@ __global__ void batched_reduce(const __grid_constant__ BatchReduceArgs a) {
         const int item = P.item0 + c * P.n_bands + band;
         acc = cadd(acc, a.partial[(((size_t)item * a.fb + fl) * a.tx_pad + t) * a.e_pad + e]);
       }
+      if (a.apply_pp) acc = cmul(acc, P.pp[f]);
       const float s = P.probe[f] * P.corr;
       acc = make_float2(acc.x * s, acc.y * s);
     }
@@ -569,6 +570,7 @@ static int32_t simus_batched_impl(const FsgProbe* probe, const FsgMedium* medium
     a.fb = L.fb;
     a.tx_pad = kBTX;
     a.e_pad = kBE;
+    a.apply_pp = 0;
     a.partial = partial;
     batched_reduce<<<dim3(2 * sms, n_phantoms), 256, 0, s>>>(a);
     if ((st = check_cuda(cudaGetLastError(), "batched_reduce launch")) != FSG_OK) return st;

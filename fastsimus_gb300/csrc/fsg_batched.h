@@ -66,6 +66,7 @@ struct BatchReduceArgs {
   BatchPhantom ph[kMaxPhantoms];
   int n_phantoms, n_tx, E, fb;
   int tx_pad, e_pad;        // partial layout [item][fb][tx_pad][e_pad]
+  int apply_pp;             // 1: the partials lack the pulse x probe factor (tensor-core path)
   const float2* partial;
 };
 

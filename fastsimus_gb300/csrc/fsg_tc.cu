@@ -8,9 +8,10 @@
 //   TX  (MMA)  D_tx[(c,s)][(c',t)] = sum_e Gc[s][e] * Dc'[e][t]     M=128 N=64 K=64
 //              with c, c' in {re, im}: rows [Gr; Gi], columns [Dr | Di]
 //              P = (D_tx[0,s][0,t] - D_tx[1,s][1,t]) + i (D_tx[0,s][1,t] + D_tx[1,s][0,t])
-//   RX  (MMA)  D_rx[f][(c,e)][(c',t)] += sum_s Wc[s][e] * Pc'[s][t]  M=128 N=64 K=64
-//              with W = Gm * rc_s * pulse * probe (rows [Wr^T; Wi^T]) and columns [Pr | Pi];
-//              Y = D_rx[0][0] - D_rx[1][1] + i (D_rx[0][1] + D_rx[1][0]) is formed once per item.
+//   RX  (MMA)  D_rx[f][(c,e)][(c',t)] += sum_s Gc[s][e] * Qc'[s][t]  M=128 N=64 K=64
+//              with rows [Gr^T; Gi^T] (the same BF16 words as the TX operand) and columns
+//              [Qr | Qi], Q = rc_s P; Y = D_rx[0][0] - D_rx[1][1] + i (D_rx[0][1] + D_rx[1][0]) is
+//              formed once per item, and the reduction multiplies it by pulse x probe.
 //
 // Each real GEMM is A_hi B_hi + A_hi B_lo + A_lo B_hi (three tcgen05.mma kind::f16 per K step).
 // TX operands are K-major; RX operands are written MN-major so that no thread transposes data.
@@ -122,7 +123,6 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
   __shared__ uint32_t tmem_holder;
   __shared__ int s_item, s_fail;
   __shared__ float rcs[kTcT];
-  __shared__ float2 pps[kTcMaxFb];
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int fb = A.fb, E = A.E, T = A.n_tx;
@@ -206,7 +206,6 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
       *reinterpret_cast<__nv_bfloat16*>(bt + off) = hi;
       *reinterpret_cast<__nv_bfloat16*>(bt + 8192 + off) = lo;
     }
-    if (tid < kTcMaxFb) pps[tid] = (tid < nf) ? P.pp[f0 + tid] : make_float2(0.f, 0.f);
     const float2 k0 = P.kf[f0];
     const float a0 = P.af[f0];
     bool first_tile = true;
@@ -236,7 +235,6 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
         }
       }
       __syncthreads();  // rcs visible
-      const float rc_s = rcs[s_g];
 
       for (int f = 0; f < nf; ++f) {
         // previous RX MMAs read A_rx / B_rx: wait before overwriting
@@ -248,12 +246,14 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
         __syncthreads();
         tc::fence_after_sync();
         if (s_fail) break;
-        const float2 sc = make_float2(rc_s * pps[f].x, rc_s * pps[f].y);
         // ---- Green's values at f; write A_tx (K-major rows (c, s), K = e) and
-        //      A_rx (MN-major rows (c, e), K = s) in halves of 8 elements ----
+        //      A_rx (MN-major rows (c, e), K = s) in halves of 8 elements.  Both operands hold
+        //      the same BF16 hi/lo words: eight consecutive elements of one scatterer are one
+        //      16-byte core-matrix row in either layout.  The receive weights rc (real) go into
+        //      B_rx and pulse x probe (one complex factor per frequency) into the reduction. ----
 #pragma unroll
         for (int half = 0; half < 2; ++half) {
-          float gr[8], gi[8], wr[8], wi[8];
+          float gr[8], gi[8];
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             const int jj = half * 8 + j;
@@ -262,8 +262,6 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
             for (int u = 1; u < U; ++u) acc = cadd(acc, G[jj * U + u]);
             gr[j] = acc.x;
             gi[j] = acc.y;
-            wr[j] = acc.x * sc.x - acc.y * sc.y;
-            wi[j] = acc.x * sc.y + acc.y * sc.x;
 #pragma unroll
             for (int u = 0; u < U; ++u) G[jj * U + u] = cmul(G[jj * U + u], S[jj * U + u]);
           }
@@ -276,8 +274,6 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
           *reinterpret_cast<uint4*>(sm + kOffAtxLo + o_re) = lr;
           *reinterpret_cast<uint4*>(sm + kOffAtxHi + o_im) = hi_;
           *reinterpret_cast<uint4*>(sm + kOffAtxLo + o_im) = li_;
-          tc::split8(wr, hr, lr);
-          tc::split8(wi, hi_, li_);
           const uint32_t q_re = tc::mnmajor_off(e0, s_g, 16), q_im = tc::mnmajor_off(64 + e0, s_g, 16);
           *reinterpret_cast<uint4*>(sm + kOffArxHi + q_re) = hr;
           *reinterpret_cast<uint4*>(sm + kOffArxLo + q_re) = lr;
@@ -318,10 +314,12 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
         }
         __syncthreads();
         if (row < 64) {
-          // h = 0: Pr = D[0,s][0,t] - D[1,s][1,t];  h = 1: Pi = D[0,s][1,t] + D[1,s][0,t]
+          // h = 0: Pr = D[0,s][0,t] - D[1,s][1,t];  h = 1: Pi = D[0,s][1,t] + D[1,s][0,t];
+          // times the scatterer's reflectivity
           const float* x = X + ((1 - h) * 64 + row) * kXPitch;
+          const float rw = rcs[row];
 #pragma unroll
-          for (int t = 0; t < 32; ++t) v[t] = h ? v[t] + x[t] : v[t] - x[t];
+          for (int t = 0; t < 32; ++t) v[t] = rw * (h ? v[t] + x[t] : v[t] - x[t]);
 #pragma unroll
           for (int c8 = 0; c8 < 4; ++c8) {
             uint4 hh, ll;
@@ -729,6 +727,7 @@ extern "C" int32_t fsg_simus_batched_tc(const FsgProbe* probe, const FsgMedium* 
     a.fb = L.fb;
     a.tx_pad = kTcTx;
     a.e_pad = kTcE;
+    a.apply_pp = 1;  // the tensor-core partials carry rc but not pulse x probe
     a.partial = partial;
     batched_reduce<<<dim3(2 * sms, n_phantoms), 256, 0, s>>>(a);
     if ((st = check_cuda(cudaGetLastError(), "batched_reduce launch")) != FSG_OK) return st;
