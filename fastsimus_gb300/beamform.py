@@ -157,13 +157,17 @@ def dasmtx(sig, x, z, param, method: str = "linear") -> torch.Tensor:
     signals (as the reference's tests pass it), a real shape for RF, or an array.  Returns a
     complex64 sparse CSR tensor of ``x.size`` rows (pixels in Fortran order of the grid) and
     ``n_samples * n_channels`` columns (the Fortran-order flattening of the signal)."""
-    s = np.asarray(sig)
-    if s.shape == (2,) and s.dtype.kind in "fc":
-        iq = bool(np.iscomplexobj(s))
-        ns, nc = (int(round(abs(v))) for v in s)
+    if isinstance(sig, torch.Tensor):
+        iq = bool(torch.is_complex(sig))
+        ns, nc = int(sig.shape[-2]), int(sig.shape[-1])
     else:
-        iq = bool(torch.is_complex(sig)) if isinstance(sig, torch.Tensor) else bool(np.iscomplexobj(s))
-        ns, nc = int(s.shape[0]), int(s.shape[1])
+        s = np.asarray(sig)
+        if s.shape == (2,) and s.dtype.kind in "fc":
+            iq = bool(np.iscomplexobj(s))
+            ns, nc = (int(round(abs(v))) for v in s)
+        else:
+            iq = bool(np.iscomplexobj(s))
+            ns, nc = int(s.shape[-2]), int(s.shape[-1])
     if nc != int(param.Nelements):
         raise ValueError(f"signal has {nc} channels but param.Nelements = {param.Nelements}")
     if param.TXdelay is None:

@@ -95,6 +95,9 @@ def test_dasmtx_matches_oracle_and_das(method):
     param = DasParam(fc=FC, pitch=pitch, Nelements=24, width=0.25e-3, c=C, fs=fs, fnumber=1.2, TXdelay=delays[1])
     m = dasmtx(1j * np.array(q[1].shape), x, z, param, method)
     assert m.layout == torch.sparse_csr and m.shape == (x.size, 600 * 24)
+    # the signal itself (a GPU tensor) instead of its shape gives the same matrix
+    m_t = dasmtx(torch.as_tensor(q[1], device="cuda"), x, z, param, method)
+    assert torch.equal(m_t.values(), m.values()) and torch.equal(m_t.col_indices(), m.col_indices())
     dense = np64(m.to_dense())
     # oracle rows are in C order of the grid; the matrix's in Fortran order, as pymust.dasmtx's
     ref = D.das_weights(600, x.reshape(-1, order="F"), z.reshape(-1, order="F"), delays[1], n_elements=24,
