@@ -132,6 +132,7 @@ _SIGNATURES = {
     "fsg_das": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgDasParams), _P, ctypes.c_int32,
                                  ctypes.c_int32, _P, _P, ctypes.c_int64, _P, _P]),
     "fsg_dasmtx_nnz_per_row": (ctypes.c_int32, [ctypes.c_int32, ctypes.c_int32]),
+    "fsg_wait_selftest": (ctypes.c_int32, [ctypes.c_int32, ctypes.c_int32, _P, _P]),
     "fsg_dasmtx": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgDasParams), ctypes.c_int32, _P, _P,
                                     ctypes.c_int64, _P, _P, _P, _P]),
 }

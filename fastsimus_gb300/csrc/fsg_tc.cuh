@@ -62,10 +62,22 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* mbar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait: returns false if the phase did not complete within `max_tries` polls.
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+constexpr uint64_t kMaxWaitNs = 2000000000ull;  // a wait gives up after 2 s, whatever max_tries
+
+// Bounded wait: returns false if the phase did not complete within `max_tries` polls or
+// kMaxWaitNs nanoseconds of the global timer, whichever comes first.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* mbar, uint32_t parity, uint32_t max_tries) {
-  for (uint32_t i = 0; i < max_tries; ++i)
+  const uint64_t t0 = global_ns();
+  for (uint32_t i = 0; i < max_tries; ++i) {
     if (mbar_try_wait(mbar, parity)) return true;
+    if ((i & 255u) == 255u && global_ns() - t0 > kMaxWaitNs) return false;
+  }
   return false;
 }
 

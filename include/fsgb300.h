@@ -362,6 +362,12 @@ int32_t fsg_dasmtx_nnz_per_row(int32_t method, int32_t n_elements);
 int32_t fsg_dasmtx(const FsgProbe* probe, const FsgDasParams* params, int32_t n_samples, const double* tx_delays,
                    const double* pixels, int64_t n_pixels, int32_t* crow, int32_t* col, void* val, void* stream);
 
+/* Check of the bounded device-side wait (no counterpart in the reference).  One thread waits,
+ * for at most max_tries polls or 2 s, on an mbarrier phase: one it completed itself when arrive
+ * != 0, else one that nothing completes.  Writes FSG_OK or FSG_ETIMEOUT to *status (device
+ * int); the context stays usable either way. */
+int32_t fsg_wait_selftest(int32_t arrive, int32_t max_tries, int32_t* status, void* stream);
+
 /* Measurement utility, no counterpart in the reference: launches `blocks` x 256 threads of
  * independent FP32 FMA chains (`iters` iterations) and reports the FLOPs it performs, so a
  * caller can time it with events and state the device's FP32 FMA roofline.  `out` must hold
