@@ -33,8 +33,8 @@ _DEFAULT_MEDIUM = MediumParams()
 
 @dataclass(frozen=True)
 class BatchTuning:
-    """Tile shapes of the batched sweep: frequencies per work item (1 or 2), scatterers per
-    work item, persistent CTAs per SM."""
+    """Tile shapes of the batched sweep: frequencies per work item (1 or 2; probes of more
+    than 64 elements always use 1), scatterers per work item, persistent CTAs per SM."""
 
     freqs_per_item: int = 2
     chunk_scatterers: int = 32768
@@ -211,7 +211,9 @@ class BatchedSimus:
         if candidates is None:
             total = sum(int(s.shape[0]) for s, _ in self.phantoms)
             chunks = sorted({c for c in (8192, 16384, 32768, 65536, 131072) if c < 2 * max(total, 64)} or {8192})
-            candidates = [BatchTuning(fb, c, 1) for fb in (1, 2) for c in chunks[:: max(1, len(chunks) // 2)]]
+            # probes of more than 64 elements use the 128-element tile, one frequency per item
+            fbs = (1,) if self.params.n_elements > 64 else (1, 2)
+            candidates = [BatchTuning(fb, c, 1) for fb in fbs for c in chunks[:: max(1, len(chunks) // 2)]]
         timings = []
         for cand in candidates:
             self.set_tuning(cand)

@@ -30,10 +30,11 @@
 namespace fsg {
 
 constexpr int kBT = 64;        // scatterers per tile
-constexpr int kBE = 64;        // padded elements
 constexpr int kBTX = 80;       // padded transmits
-constexpr int kGmPitch = 65;   // complex per Gm row (64 + 1 pad: conflict-free column reads)
 constexpr int kWPitch = 81;    // complex per W / D row
+// Elements are padded to EB = 64 or 128 (a template parameter); a Gm row holds EB + 1 complex
+// values (the pad keeps column reads conflict-free).
+__host__ __device__ constexpr int gm_pitch(int eb) { return eb + 1; }
 
 __device__ __forceinline__ void df_mul_exact(float a, float b, float& p, float& e) {
   p = __fmul_rn(a, b);
@@ -55,12 +56,15 @@ __device__ __forceinline__ float2 cis_two_pi_ftau(float2 f, float2 tau) {
   return make_float2(c, s);
 }
 
-template <int FB>
+// EB padded elements: the receive register tile is EB/16 element rows x 5 transmits per thread.
+template <int FB, int EB>
 __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_constant__ BatchArgs A) {
   extern __shared__ __align__(16) unsigned char sm[];
+  constexpr int kGmPitch = gm_pitch(EB);
+  constexpr int kRows = EB / 16;                                     // receive rows per thread
   float2* Gm = reinterpret_cast<float2*>(sm);                       // [FB][kBT][kGmPitch]
-  float2* D = Gm + FB * kBT * kGmPitch;                              // [FB][kBE][kWPitch]
-  float2* W = D + FB * kBE * kWPitch;                                // [kBT][kWPitch]
+  float2* D = Gm + FB * kBT * kGmPitch;                              // [FB][EB][kWPitch]
+  float2* W = D + FB * EB * kWPitch;                                 // [kBT][kWPitch]
   float* rcs = reinterpret_cast<float*>(W + kBT * kWPitch);          // [kBT]
   __shared__ int s_item;
 
@@ -87,8 +91,8 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
     const int64_t s_end = min(P.n_scat, s_begin + A.chunk);
 
     // --- transmit matrices D[f][e][t] for the band (exact, per item) ---
-    for (int i = tid; i < FB * kBE * kBTX; i += kThreads) {
-      const int f = i / (kBE * kBTX), r = i % (kBE * kBTX), e = r / kBTX, t = r % kBTX;
+    for (int i = tid; i < FB * EB * kBTX; i += kThreads) {
+      const int f = i / (EB * kBTX), r = i % (EB * kBTX), e = r / kBTX, t = r % kBTX;
       float2 v = make_float2(0.f, 0.f);
       if (f < nf && e < E && t < T) {
         const float2 tau = A.tau[t * E + e];  // double-float seconds, NaN already mapped to 0
@@ -99,7 +103,7 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
           v = make_float2(w * c.x, w * c.y);
         }
       }
-      D[(f * kBE + e) * kWPitch + t] = v;
+      D[(f * EB + e) * kWPitch + t] = v;
     }
     // band constants
     float2 pp[FB];
@@ -111,11 +115,11 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
     C.dk = P.dk;
     C.dalpha = P.dalpha;
 
-    float2 Y[FB][4][5];
+    float2 Y[FB][kRows][5];
 #pragma unroll
     for (int f = 0; f < FB; ++f)
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
+      for (int i = 0; i < kRows; ++i)
 #pragma unroll
         for (int j = 0; j < 5; ++j) Y[f][i][j] = make_float2(0.f, 0.f);
 
@@ -133,12 +137,13 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
         rcs[tid] = w;
       }
       __syncthreads();
-      // --- Green's matrix Gm[f][s][e] for the tile: thread (e, s-group of 16) ---
+      // --- Green's matrix Gm[f][s][e] for the tile: thread (e, s-group of kBT * EB / 256) ---
       {
-        const int e = tid & 63;
-        const int sg = tid >> 6;
-        for (int k = 0; k < 16; ++k) {
-          const int sl = sg * 16 + k;
+        constexpr int kSpg = kBT * EB / kThreads;
+        const int e = tid % EB;
+        const int sg = tid / EB;
+        for (int k = 0; k < kSpg; ++k) {
+          const int sl = sg * kSpg + k;
           const int64_t s = t0 + sl;
           float2 g0 = make_float2(0.f, 0.f), g1 = make_float2(0.f, 0.f);
           if (e < E && s < s_end) {
@@ -178,9 +183,9 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
           for (int i = 0; i < 4; ++i)
   #pragma unroll
             for (int j = 0; j < 5; ++j) acc[i][j] = make_float2(0.f, 0.f);
-          const float2* Df = D + f * kBE * kWPitch;
+          const float2* Df = D + f * EB * kWPitch;
   #pragma unroll 4
-          for (int e = 0; e < kBE; ++e) {
+          for (int e = 0; e < EB; ++e) {
             float2 a[4], b[5];
   #pragma unroll
             for (int i = 0; i < 4; ++i) a[i] = G[(wm * 16 + lm + 4 * i) * kGmPitch + e];
@@ -202,16 +207,16 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
           }
         }
         __syncthreads();
-        // --- RX: Y[e][t] += sum_s G[s][e] W[s][t]; thread rows e = wm*16 + lm + 4i
+        // --- RX: Y[e][t] += sum_s G[s][e] W[s][t]; thread rows e = wm*(EB/4) + lm + 4i
 #pragma unroll 4
         for (int s = 0; s < kBT; ++s) {
-          float2 a[4], b[5];
+          float2 a[kRows], b[5];
 #pragma unroll
-          for (int i = 0; i < 4; ++i) a[i] = G[s * kGmPitch + wm * 16 + lm + 4 * i];
+          for (int i = 0; i < kRows; ++i) a[i] = G[s * kGmPitch + wm * (EB / 4) + lm + 4 * i];
 #pragma unroll
           for (int j = 0; j < 5; ++j) b[j] = W[s * kWPitch + wn * 40 + ln * 5 + j];
 #pragma unroll
-          for (int i = 0; i < 4; ++i)
+          for (int i = 0; i < kRows; ++i)
 #pragma unroll
             for (int j = 0; j < 5; ++j) Y[f][i][j] = cfma(a[i], b[j], Y[f][i][j]);
         }
@@ -219,15 +224,15 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
       }
     }
     // --- partial spectrum of this item: [item][f][t][e] ---
-    float2* out = A.partial + (size_t)item * FB * kBTX * kBE;
+    float2* out = A.partial + (size_t)item * FB * kBTX * EB;
 #pragma unroll
     for (int f = 0; f < FB; ++f)
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
+      for (int i = 0; i < kRows; ++i)
 #pragma unroll
         for (int j = 0; j < 5; ++j) {
-          const int e = wm * 16 + lm + 4 * i, t = wn * 40 + ln * 5 + j;
-          out[((size_t)f * kBTX + t) * kBE + e] = Y[f][i][j];
+          const int e = wm * (EB / 4) + lm + 4 * i, t = wn * 40 + ln * 5 + j;
+          out[((size_t)f * kBTX + t) * EB + e] = Y[f][i][j];
         }
   }
 }
@@ -319,23 +324,24 @@ __global__ void __launch_bounds__(kThreads) batched_geometry_kernel(const __grid
   }
 }
 
-size_t batched_smem_bytes(int fb) {
-  return (size_t)(fb * kBT * kGmPitch + fb * kBE * kWPitch + kBT * kWPitch) * sizeof(float2) + kBT * sizeof(float);
+size_t batched_smem_bytes(int fb, int eb) {
+  return (size_t)(fb * kBT * gm_pitch(eb) + fb * eb * kWPitch + kBT * kWPitch) * sizeof(float2) + kBT * sizeof(float);
 }
 
-cudaError_t launch_batched(int fb, int grid, const BatchArgs& A, cudaStream_t s) {
-  const size_t smem = batched_smem_bytes(fb);
-  cudaError_t e;
-  if (fb == 1) {
-    e = cudaFuncSetAttribute(batched_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    batched_kernel<1><<<grid, kThreads, smem, s>>>(A);
-  } else {
-    e = cudaFuncSetAttribute(batched_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    batched_kernel<2><<<grid, kThreads, smem, s>>>(A);
-  }
+int batched_pad_elements(int n_elements) { return n_elements <= 64 ? 64 : 128; }
+
+template <int FB, int EB>
+static cudaError_t launch_batched_t(int grid, const BatchArgs& A, cudaStream_t s) {
+  const size_t smem = batched_smem_bytes(FB, EB);
+  cudaError_t e = cudaFuncSetAttribute(batched_kernel<FB, EB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  batched_kernel<FB, EB><<<grid, kThreads, smem, s>>>(A);
   return cudaGetLastError();
+}
+
+cudaError_t launch_batched(int fb, int eb, int grid, const BatchArgs& A, cudaStream_t s) {
+  if (eb == 128) return launch_batched_t<1, 128>(grid, A, s);  // the 128-element tile fits one frequency
+  return fb == 1 ? launch_batched_t<1, 64>(grid, A, s) : launch_batched_t<2, 64>(grid, A, s);
 }
 
 }  // namespace fsg
@@ -351,7 +357,7 @@ using namespace fsg;
 size_t a256(size_t v) { return (v + 255) & ~size_t(255); }
 
 struct BatchPlanLayout {
-  int fb, chunk, n_items;
+  int fb, eb, chunk, n_items;
   int n_bands[kMaxPhantoms], n_chunks[kMaxPhantoms], item0[kMaxPhantoms];
   int64_t geo0[kMaxPhantoms], max_scat;
   size_t off_src, off_rot, off_tau, off_apod, off_queue, off_tab[kMaxPhantoms], off_partial, off_geo_a, off_geo_b,
@@ -360,7 +366,9 @@ struct BatchPlanLayout {
 
 int plan_layout(const FsgProbe* probe, const FsgPhantom* ph, int n_ph, int n_tx, const FsgBatchTuning* tu,
                 BatchPlanLayout* L) {
-  L->fb = (tu && tu->freqs_per_item == 1) ? 1 : 2;
+  L->eb = batched_pad_elements(probe->n_elements);
+  // two frequencies per item only fit the 64-element tile's shared memory
+  L->fb = (L->eb > 64 || (tu && tu->freqs_per_item == 1)) ? 1 : 2;
   int64_t chunk = (tu && tu->chunk_scatterers > 0) ? tu->chunk_scatterers : 32768;
   chunk = ((chunk + kBT - 1) / kBT) * kBT;
   L->chunk = (int)chunk;
@@ -388,7 +396,7 @@ int plan_layout(const FsgProbe* probe, const FsgPhantom* ph, int n_ph, int n_tx,
   }
   L->n_items = items;
   L->off_partial = o;
-  o += a256((size_t)items * L->fb * kBTX * kBE * 8);
+  o += a256((size_t)items * L->fb * kBTX * L->eb * 8);
   L->off_geo_a = o;
   o += a256((size_t)scat * E * U * 16);
   L->off_geo_b = o;
@@ -559,7 +567,7 @@ static int32_t simus_batched_impl(const FsgProbe* probe, const FsgMedium* medium
     const int per_sm = (tuning && tuning->ctas_per_sm > 0) ? tuning->ctas_per_sm : 1;
     int grid = sms * per_sm;
     if (grid > L.n_items) grid = L.n_items;
-    if ((st = check_cuda(launch_batched(L.fb, grid, A, s), "batched_kernel launch")) != FSG_OK) return st;
+    if ((st = check_cuda(launch_batched(L.fb, L.eb, grid, A, s), "batched_kernel launch")) != FSG_OK) return st;
   }
   {
     BatchReduceArgs a;
@@ -569,7 +577,7 @@ static int32_t simus_batched_impl(const FsgProbe* probe, const FsgMedium* medium
     a.E = E;
     a.fb = L.fb;
     a.tx_pad = kBTX;
-    a.e_pad = kBE;
+    a.e_pad = L.eb;
     a.apply_pp = 0;
     a.partial = partial;
     batched_reduce<<<dim3(2 * sms, n_phantoms), 256, 0, s>>>(a);

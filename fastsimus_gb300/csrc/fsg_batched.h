@@ -9,7 +9,7 @@
 namespace fsg {
 
 constexpr int kMaxPhantoms = 64;
-constexpr int kBatchMaxE = 64;
+constexpr int kBatchMaxE = 128;
 constexpr int kBatchMaxTx = 80;
 
 struct BatchPhantom {
@@ -70,9 +70,11 @@ struct BatchReduceArgs {
   const float2* partial;
 };
 
-size_t batched_smem_bytes(int fb);
+size_t batched_smem_bytes(int fb, int eb);
+// Padded element count of the FP32 batched kernel's tiles (64 or 128).
+int batched_pad_elements(int n_elements);
 __global__ void batched_geometry_kernel(const __grid_constant__ BatchArgs A);
-cudaError_t launch_batched(int fb, int grid, const BatchArgs& A, cudaStream_t s);
+cudaError_t launch_batched(int fb, int eb, int grid, const BatchArgs& A, cudaStream_t s);
 __global__ void batched_setup(const __grid_constant__ BatchSetupArgs a);
 __global__ void batched_reduce(const __grid_constant__ BatchReduceArgs a);
 

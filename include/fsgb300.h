@@ -165,7 +165,8 @@ size_t fsg_simus_batched_workspace_size(const FsgProbe* probe, const FsgPhantom*
  * (tests/_picmus_phantom_shared.py:319-367, step body _simus_strategies.py:23-77): the
  * Green's terms of each (scatterer, element, frequency) are generated once and contracted with
  * every transmit.  delays/apod are device [n_tx][n_elements] float64 (apod NULL = ones; NaN
- * delay = element off).  Limits of this build: n_elements <= 64, n_tx <= 80, n_phantoms <= 64.
+ * delay = element off).  Limits of this build: n_elements <= 128 (probes of 65-128 elements use a
+ * 128-element tile with one frequency per work item), n_tx <= 80, n_phantoms <= 64.
  * Phantom descriptors travel as a kernel parameter, so the call contains no host-to-device
  * copy and can be captured in a CUDA graph.
  */

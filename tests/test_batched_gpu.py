@@ -96,10 +96,35 @@ def test_batched_rejects_unsupported_shapes():
     from fastsimus_gb300 import workloads as W
     from fastsimus_gb300.batched import BatchedSimus
 
-    p2, m2 = W.cfg2_probe(), W.cfg2_medium()  # 128 elements > 64
-    s, r = W.cfg2_scatterers(100)
-    with pytest.raises(NotImplementedError):
-        BatchedSimus([(s, r)], np.zeros((2, 128)), p2, m2).run()
+    p, m = W.cfg1_probe(), W.cfg1_medium()
+    s, r = W.cfg1_scatterers(100)
+    with pytest.raises(NotImplementedError):  # 81 firings > 80
+        BatchedSimus([(s, r)], np.zeros((81, 64)), p, m).run()
+
+
+@pytest.mark.parametrize("n_elements", [128, 96])
+def test_batched_128_element_tile_vs_oracle(n_elements):
+    """Probes of 65-128 elements use the 128-element tile (one frequency per item): the
+    config-2 L11 probe, and a 96-element array whose tile is a third padding."""
+    import dataclasses
+
+    from fastsimus_gb300 import workloads as W
+    from fastsimus_gb300.batched import BatchedSimus
+
+    p, m = W.cfg2_probe(), W.cfg2_medium()
+    p = dataclasses.replace(p, n_elements=n_elements)
+    rng = np.random.default_rng(5)
+    phantoms = [(W.uniform_box(rng, n, (-8e-3, 8e-3), (6e-3, 30e-3)), rng.standard_normal(n)) for n in (120, 45)]
+    delays = W.plane_wave_delays(p, m, [-8.0, 0.0, 6.0])
+    b = BatchedSimus(phantoms, delays, p, m)
+    res = b.run()
+    for (sc, rc), plan, out in zip(phantoms, b.plans, res):
+        rf = np64(out.rf)
+        assert rf.shape[1] == n_elements
+        for t in range(delays.shape[0]):
+            ref = O.simus_compute(sc, rc, delays[t], plan, p, m)
+            err = G.rel_l2(rf[:, :, t], ref.rf)
+            assert err < PLAIN_TOL, (t, err)
 
 
 def test_batched_phantom_without_scatterers_gives_zero():
