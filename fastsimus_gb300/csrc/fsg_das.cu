@@ -236,7 +236,7 @@ __device__ __forceinline__ bool das_tap(const DasArgs& A, const DasShared& S, in
 // registers / local memory), then per element the receive distance, aperture test and rotation
 // once, and per firing only the sample gather, the interpolation and one complex multiply-add.
 // The group's transmit delays (times c) sit in dynamic shared memory, [firing][element].
-__global__ void __launch_bounds__(kDasImgThreads) das_kernel(const __grid_constant__ DasArgs A, int group) {
+__global__ void __launch_bounds__(kDasImgThreads, 4) das_kernel(const __grid_constant__ DasArgs A, int group) {
   __shared__ DasShared S;
   extern __shared__ float ctx_g[];  // [group][E]
   das_load_elements(A, S);
@@ -278,24 +278,35 @@ __global__ void __launch_bounds__(kDasImgThreads) das_kernel(const __grid_consta
       const float dr = sqrtf(fmaf(dx, dx, dz * dz));
       float2 ae = make_float2(0.f, 0.f);
       const float2* ce = A.iq + ((size_t)g0 * A.E + e) * A.n_s;
-      for (int j = 0; j < ng; ++j, ce += (size_t)A.E * A.n_s) {
-        const float t = (dtx[j] + dr) * A.inv_c;
-        const float s = (t - A.t0) * A.fs;
-        float2 v;
-        if (A.method == FSG_DAS_LINEAR) {
+      const size_t fstride = (size_t)A.E * A.n_s;
+      const float last = (float)(A.n_s - 1);
+      // branch-free taps (a tap outside the record reads sample 0 with weight 0), unrolled so
+      // that the gathers of several firings are in flight together
+      if (A.method == FSG_DAS_LINEAR) {
+#pragma unroll 4
+        for (int j = 0; j < ng; ++j) {
+          const float s = ((dtx[j] + dr) * A.inv_c - A.t0) * A.fs;
           const float fi = floorf(s);
-          if (!(fi >= 0.f) || !(fi + 1.f <= (float)(A.n_s - 1))) continue;
-          const int i0 = (int)fi;
+          const bool ok = fi >= 0.f && fi + 1.f <= last;
+          const int i0 = ok ? (int)fi : 0;
           const float w = s - fi;
-          const float2 a = ce[i0], b = ce[i0 + 1];
-          v = make_float2(fmaf(w, b.x - a.x, a.x), fmaf(w, b.y - a.y, a.y));
-        } else {
-          const float fi = floorf(s + 0.5f);
-          if (!(fi >= 0.f) || !(fi <= (float)(A.n_s - 1))) continue;
-          v = ce[(int)fi];
+          const float2* cj = ce + j * fstride;
+          const float2 a = cj[i0], b = cj[i0 + 1];
+          const float2 v = ok ? make_float2(fmaf(w, b.x - a.x, a.x), fmaf(w, b.y - a.y, a.y)) : make_float2(0.f, 0.f);
+          ae.x = fmaf(v.x, rtx[j].x, fmaf(-v.y, rtx[j].y, ae.x));
+          ae.y = fmaf(v.x, rtx[j].y, fmaf(v.y, rtx[j].x, ae.y));
         }
-        ae.x = fmaf(v.x, rtx[j].x, fmaf(-v.y, rtx[j].y, ae.x));
-        ae.y = fmaf(v.x, rtx[j].y, fmaf(v.y, rtx[j].x, ae.y));
+      } else {
+#pragma unroll 4
+        for (int j = 0; j < ng; ++j) {
+          const float s = ((dtx[j] + dr) * A.inv_c - A.t0) * A.fs;
+          const float fi = floorf(s + 0.5f);
+          const bool ok = fi >= 0.f && fi <= last;
+          const float2 c = ce[j * fstride + (ok ? (int)fi : 0)];
+          const float2 v = ok ? c : make_float2(0.f, 0.f);
+          ae.x = fmaf(v.x, rtx[j].x, fmaf(-v.y, rtx[j].y, ae.x));
+          ae.y = fmaf(v.x, rtx[j].y, fmaf(v.y, rtx[j].x, ae.y));
+        }
       }
       float sn = 0.f, cs = 1.f;
       if (A.iq_rot) sincospif(2.f * k_cyc * dr, &sn, &cs);
