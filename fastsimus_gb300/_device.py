@@ -28,9 +28,11 @@ def pick_device(*arrays) -> torch.device:
 
 
 def to_dev_f64(a, device: torch.device, shape=None) -> torch.Tensor:
-    """Contiguous float64 tensor on `device` (copies host arrays in)."""
+    """Contiguous float64 tensor on `device` (copies host arrays in).  A pinned host tensor is
+    copied asynchronously on the current stream, so the caller must leave it unchanged until the
+    stream has passed the call; other host inputs are copied synchronously."""
     if isinstance(a, torch.Tensor):
-        t = a.to(device=device, dtype=torch.float64)
+        t = a.to(device=device, dtype=torch.float64, non_blocking=(not a.is_cuda) and a.is_pinned())
     else:
         t = torch.as_tensor(np.asarray(a, dtype=np.float64), device=device)
     if shape is not None:
