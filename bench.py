@@ -658,7 +658,9 @@ def run_batched_workload(args):
     t0 = time.perf_counter()
     from fastsimus_gb300.batched import BatchTuning
 
-    quick = [BatchTuning(1, 65536, 1), BatchTuning(2, 65536, 1)] if getattr(args, "autotune_quick", False) else None
+    # the quick list holds the shapes the full autotune settles on for this workload
+    quick = ([BatchTuning(2, 8192, 1), BatchTuning(1, 8192, 1), BatchTuning(2, 32768, 1)]
+             if getattr(args, "autotune_quick", False) else None)
     best = b.autotune(candidates=quick, cache=False)
     t_tune = time.perf_counter() - t0
     b.capture()
