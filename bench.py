@@ -596,7 +596,8 @@ def run_beamform_workload(args):
     torch.cuda.synchronize()
     t_iq, t_das = [], []
     with ClockSampler(device.index or 0) as clocks:
-        for _ in range(max(args.steps, 3)):
+        # ~0.5 s of steps, so the clock sampler (every 200 ms) sees the timed region
+        for _ in range(max(args.steps, 300)):
             flush.zero_()
             ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
             step(ev)
