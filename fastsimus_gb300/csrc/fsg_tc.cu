@@ -34,14 +34,18 @@ namespace fsg {
 
 constexpr int kTcT = 64;        // scatterers per tile
 constexpr int kTcE = 64;        // padded elements
-constexpr int kTcTx = 32;       // padded transmits
-constexpr int kTcMaxFb = 7;     // TMEM: 64 (TX) + 64 per band frequency <= 512 columns
+constexpr int kTcTxChunk = 32;  // transmits per column chunk: an accumulator has N = 64 nc columns
+constexpr int kTcMaxTx = 96;    // up to nc = 3 chunks
+constexpr int kTcMaxFb = 7;     // TMEM: N (TX) + N per band frequency <= 512 columns
+// Band frequencies per item that fit TMEM with nc transmit chunks: 7, 3, 1.
+__host__ __device__ constexpr int tc_max_fb(int nc) { return 512 / (64 * nc) - 1; }
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kWaitTries = 1u << 26;
 
 struct TcArgs {
   BatchPhantom ph[kMaxPhantoms];
   int n_phantoms, n_items, E, U, n_tx, fb, convex;
+  int nc;           // transmit chunks of 32: N = 64 nc accumulator columns
   int64_t chunk;
   const float4* src_pos;
   const float2* rot_e;
@@ -51,7 +55,7 @@ struct TcArgs {
   double apex, radius2;
   int* queue;
   int* status;
-  float2* partial;  // [n_items][fb][kTcTx][kTcE]
+  float2* partial;  // [n_items][fb][32 nc][kTcE]
   const float4* geo;  // per (tile, state, thread) geometry of all phantoms, see tc_geometry_kernel
 };
 
@@ -106,15 +110,26 @@ constexpr uint32_t kOffAtxHi = 0;                 // K-major  128 x 64 bf16
 constexpr uint32_t kOffAtxLo = 16384;
 constexpr uint32_t kOffArxHi = 32768;             // MN-major 128 x 64 bf16
 constexpr uint32_t kOffArxLo = 49152;
-constexpr uint32_t kOffBrxHi = 65536;             // MN-major 64 (n) x 64 (k)
-constexpr uint32_t kOffBrxLo = 73728;
-constexpr uint32_t kOffX = 81920;                 // exchange: 2 x 64 rows x 33 floats (padded: conflict-free)
 constexpr int kXPitch = 33;
-constexpr uint32_t kOffBtx = 99328;               // per band frequency: K-major 64 x 64, hi then lo
-static_assert(kOffX + 2 * 64 * kXPitch * 4 <= kOffBtx, "exchange buffer overlaps the transmit operands");
-constexpr uint32_t kBtxBytes = 16384;
-
-__host__ __device__ constexpr uint32_t tc_smem_bytes(int fb) { return kOffBtx + (uint32_t)fb * kBtxBytes + 1024; }
+// The rest depends on the transmit chunks nc (N = 64 nc): B_rx MN-major N (n) x 64 (k), hi
+// then lo; the exchange buffer, 2 x 64 rows x 33 floats (padded: conflict-free); per band
+// frequency B_tx K-major N x 64, hi then lo.
+struct TcSmem {
+  uint32_t brx_hi, brx_lo, x, btx, btx_bytes;
+};
+__host__ __device__ inline TcSmem tc_smem(int nc) {
+  TcSmem L;
+  L.brx_hi = 65536;
+  L.brx_lo = 65536 + 8192u * nc;
+  L.x = 65536 + 16384u * nc;
+  L.btx = ((L.x + 2u * 64u * kXPitch * 4u + 1023u) / 1024u) * 1024u;
+  L.btx_bytes = 16384u * nc;
+  return L;
+}
+__host__ __device__ inline uint32_t tc_smem_bytes(int fb, int nc) {
+  const TcSmem L = tc_smem(nc);
+  return L.btx + (uint32_t)fb * L.btx_bytes + 1024;
+}
 
 template <int U>
 __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__ TcArgs A) {
@@ -126,6 +141,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int fb = A.fb, E = A.E, T = A.n_tx;
+  const int NC = A.nc, NT = kTcTxChunk * NC, N = 2 * NT;
+  const TcSmem SL = tc_smem(NC);
   if (tid == 0) {
     tc::mbar_init(&mbar_tx, 1);
     tc::mbar_init(&mbar_rx, 1);
@@ -142,10 +159,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
   bool rx_pending = false;
 
   const uint32_t sbase = tc::smem_u32(sm);
-  const uint32_t id_tx = tc::idesc_bf16(128, 64, 0, 0);  // A K-major, B K-major
-  const uint32_t id_rx = tc::idesc_bf16(128, 64, 1, 1);  // A MN-major, B MN-major
-  float* X = reinterpret_cast<float*>(sm + kOffX);
-  float4* stage = reinterpret_cast<float4*>(sm + kOffAtxHi);  // geometry staging (A_tx region)
+  const uint32_t id_tx = tc::idesc_bf16(128, N, 0, 0);  // A K-major, B K-major
+  const uint32_t id_rx = tc::idesc_bf16(128, N, 1, 1);  // A MN-major, B MN-major
+  float* X = reinterpret_cast<float*>(sm + SL.x);
 
   const int s_g = tc_sg(tid), eg = tc_eg(tid);
   // TMEM read mapping: lane quarter q (rows 32q..32q+31), column half h
@@ -180,9 +196,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
     C.dalpha = P.dalpha;
 
     // ---- B_tx for the band: K-major rows n' = (c', t), K = e; value D_c'(e, t) ----
-    for (int i = tid; i < fb * 64 * 64; i += kThreads) {
-      const int f = i >> 12, n = (i >> 6) & 63, e = i & 63;
-      const int c = n >> 5, t = n & 31;
+    for (int i = tid; i < fb * N * 64; i += kThreads) {
+      const int f = i / (N * 64), n = (i >> 6) % N, e = i & 63;
+      const int c = n / NT, t = n % NT;
       float v = 0.f;
       if (f < nf && e < E && t < T) {
         const float w = A.apod[t * E + e];
@@ -201,10 +217,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
       }
       __nv_bfloat16 hi, lo;
       tc::split_bf16(v, hi, lo);
-      unsigned char* bt = sm + kOffBtx + f * kBtxBytes;
+      unsigned char* bt = sm + SL.btx + f * SL.btx_bytes;
       const uint32_t off = tc::kmajor_off(n, e, 8);
       *reinterpret_cast<__nv_bfloat16*>(bt + off) = hi;
-      *reinterpret_cast<__nv_bfloat16*>(bt + 8192 + off) = lo;
+      *reinterpret_cast<__nv_bfloat16*>(bt + SL.btx_bytes / 2 + off) = lo;
     }
     const float2 k0 = P.kf[f0];
     const float a0 = P.af[f0];
@@ -286,13 +302,13 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
         tc::fence_after_sync();
         // ---- TX MMAs ----
         if (tid == 0) {
-          const uint32_t bt = sbase + kOffBtx + f * kBtxBytes;
+          const uint32_t bt = sbase + SL.btx + f * SL.btx_bytes;
 #pragma unroll
           for (int ks = 0; ks < 4; ++ks) {
             const uint64_t ah = tc::sdesc(sbase + kOffAtxHi + ks * 256, 128, 1024);
             const uint64_t al = tc::sdesc(sbase + kOffAtxLo + ks * 256, 128, 1024);
             const uint64_t bh = tc::sdesc(bt + ks * 256, 128, 1024);
-            const uint64_t bl = tc::sdesc(bt + 8192 + ks * 256, 128, 1024);
+            const uint64_t bl = tc::sdesc(bt + SL.btx_bytes / 2 + ks * 256, 128, 1024);
             tc::mma_bf16(tmem, ah, bh, id_tx, ks > 0);
             tc::mma_bf16(tmem, ah, bl, id_tx, 1);
             tc::mma_bf16(tmem, al, bh, id_tx, 1);
@@ -304,30 +320,34 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
         __syncthreads();
         tc::fence_after_sync();
         if (s_fail) break;
-        // ---- P = combine(D_tx); write B_rx (MN-major rows n' = (c', t), K = s) ----
-        float v[32];
-        tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + 32 * h, v);
+        // ---- P = combine(D_tx); write B_rx (MN-major rows n' = (c', t), K = s), one chunk
+        //      of 32 transmits at a time ----
         const int row = 32 * q + lane;  // (c, s) with c = row / 64
-        if (row >= 64) {
+        for (int k = 0; k < NC; ++k) {
+          float v[32];
+          tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + h * NT + 32 * k, v);
+          if (row >= 64) {
 #pragma unroll
-          for (int t = 0; t < 32; ++t) X[(h * 64 + (row - 64)) * kXPitch + t] = v[t];
-        }
-        __syncthreads();
-        if (row < 64) {
-          // h = 0: Pr = D[0,s][0,t] - D[1,s][1,t];  h = 1: Pi = D[0,s][1,t] + D[1,s][0,t];
-          // times the scatterer's reflectivity
-          const float* x = X + ((1 - h) * 64 + row) * kXPitch;
-          const float rw = rcs[row];
-#pragma unroll
-          for (int t = 0; t < 32; ++t) v[t] = rw * (h ? v[t] + x[t] : v[t] - x[t]);
-#pragma unroll
-          for (int c8 = 0; c8 < 4; ++c8) {
-            uint4 hh, ll;
-            tc::split8(v + 8 * c8, hh, ll);
-            const uint32_t o = tc::mnmajor_off(32 * h + 8 * c8, row, 8);
-            *reinterpret_cast<uint4*>(sm + kOffBrxHi + o) = hh;
-            *reinterpret_cast<uint4*>(sm + kOffBrxLo + o) = ll;
+            for (int t = 0; t < 32; ++t) X[(h * 64 + (row - 64)) * kXPitch + t] = v[t];
           }
+          __syncthreads();
+          if (row < 64) {
+            // h = 0: Pr = D[0,s][0,t] - D[1,s][1,t];  h = 1: Pi = D[0,s][1,t] + D[1,s][0,t];
+            // times the scatterer's reflectivity
+            const float* x = X + ((1 - h) * 64 + row) * kXPitch;
+            const float rw = rcs[row];
+#pragma unroll
+            for (int t = 0; t < 32; ++t) v[t] = rw * (h ? v[t] + x[t] : v[t] - x[t]);
+#pragma unroll
+            for (int c8 = 0; c8 < 4; ++c8) {
+              uint4 hh, ll;
+              tc::split8(v + 8 * c8, hh, ll);
+              const uint32_t o = tc::mnmajor_off(h * NT + 32 * k + 8 * c8, row, N / 8);
+              *reinterpret_cast<uint4*>(sm + SL.brx_hi + o) = hh;
+              *reinterpret_cast<uint4*>(sm + SL.brx_lo + o) = ll;
+            }
+          }
+          if (k + 1 < NC) __syncthreads();  // X is reused by the next chunk
         }
         tc::fence_proxy_async_smem();
         tc::fence_before_sync();
@@ -335,13 +355,14 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
         tc::fence_after_sync();
         // ---- RX MMAs into this frequency's accumulator ----
         if (tid == 0) {
-          const uint32_t d = tmem + 64 + 64 * f;
+          const uint32_t d = tmem + N + N * f;
 #pragma unroll
           for (int ks = 0; ks < 4; ++ks) {
             const uint64_t ah = tc::sdesc(sbase + kOffArxHi + ks * 2 * 2048, 2048, 128);
             const uint64_t al = tc::sdesc(sbase + kOffArxLo + ks * 2 * 2048, 2048, 128);
-            const uint64_t bh = tc::sdesc(sbase + kOffBrxHi + ks * 2 * 1024, 1024, 128);
-            const uint64_t bl = tc::sdesc(sbase + kOffBrxLo + ks * 2 * 1024, 1024, 128);
+            const uint32_t lbo = 16u * N;  // N / 8 core matrices of 128 bytes per K group
+            const uint64_t bh = tc::sdesc(sbase + SL.brx_hi + ks * 2 * lbo, lbo, 128);
+            const uint64_t bl = tc::sdesc(sbase + SL.brx_lo + ks * 2 * lbo, lbo, 128);
             tc::mma_bf16(d, ah, bh, id_rx, (first_tile && ks == 0) ? 0u : 1u);
             tc::mma_bf16(d, ah, bl, id_rx, 1);
             tc::mma_bf16(d, al, bh, id_rx, 1);
@@ -363,27 +384,29 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
     __syncthreads();
     tc::fence_after_sync();
     const bool fail = s_fail != 0;
-    float2* out = A.partial + (size_t)item * fb * kTcTx * kTcE;
+    float2* out = A.partial + (size_t)item * fb * NT * kTcE;
     for (int f = 0; f < fb; ++f) {
-      float v[32];
-      const bool have = !first_tile && f < nf && !fail;
-      if (have) tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + 64 + 64 * f + 32 * h, v);
-      const int row = 32 * q + lane;  // (c, e)
-      if (row >= 64) {
+      for (int k = 0; k < NC; ++k) {
+        float v[32];
+        const bool have = !first_tile && f < nf && !fail;
+        if (have) tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + N + N * f + h * NT + 32 * k, v);
+        const int row = 32 * q + lane;  // (c, e)
+        if (row >= 64) {
 #pragma unroll
-        for (int t = 0; t < 32; ++t) X[(h * 64 + (row - 64)) * kXPitch + t] = have ? v[t] : 0.f;
-      }
-      __syncthreads();
-      if (row < 64) {
-        const float* x = X + ((1 - h) * 64 + row) * kXPitch;
-#pragma unroll
-        for (int t = 0; t < 32; ++t) {
-          const float val = have ? (h ? v[t] + x[t] : v[t] - x[t]) : 0.f;
-          float* o = reinterpret_cast<float*>(out + ((size_t)f * kTcTx + t) * kTcE + row);
-          o[h] = val;  // h = 0 real part, h = 1 imaginary part
+          for (int t = 0; t < 32; ++t) X[(h * 64 + (row - 64)) * kXPitch + t] = have ? v[t] : 0.f;
         }
+        __syncthreads();
+        if (row < 64) {
+          const float* x = X + ((1 - h) * 64 + row) * kXPitch;
+#pragma unroll
+          for (int t = 0; t < 32; ++t) {
+            const float val = have ? (h ? v[t] + x[t] : v[t] - x[t]) : 0.f;
+            float* o = reinterpret_cast<float*>(out + ((size_t)f * NT + 32 * k + t) * kTcE + row);
+            o[h] = val;  // h = 0 real part, h = 1 imaginary part
+          }
+        }
+        __syncthreads();
       }
-      __syncthreads();
     }
   }
   // ---- release TMEM ----
@@ -503,7 +526,7 @@ cudaError_t launch_tc_geometry(int U, int max_tiles, int sms, const TcArgs& A, c
 }
 
 cudaError_t launch_tc(int U, int grid, const TcArgs& A, cudaStream_t s) {
-  const uint32_t smem = tc_smem_bytes(A.fb);
+  const uint32_t smem = tc_smem_bytes(A.fb, A.nc);
   cudaError_t e;
   if (U == 1) {
     e = cudaFuncSetAttribute(tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -530,7 +553,7 @@ using namespace fsg;
 size_t tc_a256(size_t v) { return (v + 255) & ~size_t(255); }
 
 struct TcLayout {
-  int fb, chunk, n_items, max_tiles;
+  int fb, nc, chunk, n_items, max_tiles;
   int n_bands[kMaxPhantoms], n_chunks[kMaxPhantoms], item0[kMaxPhantoms];
   int64_t tile0[kMaxPhantoms];
   size_t off_src, off_rot, off_tau, off_apod, off_queue, off_tab[kMaxPhantoms], off_partial, off_geo, total;
@@ -538,8 +561,9 @@ struct TcLayout {
 
 void tc_layout(const FsgProbe* probe, const FsgPhantom* ph, int n_ph, int n_tx, const FsgBatchTuning* tu,
                TcLayout* L) {
-  int fb = (tu && tu->freqs_per_item > 0) ? tu->freqs_per_item : 7;
-  if (fb > kTcMaxFb) fb = kTcMaxFb;
+  L->nc = (n_tx + kTcTxChunk - 1) / kTcTxChunk;
+  int fb = (tu && tu->freqs_per_item > 0) ? tu->freqs_per_item : kTcMaxFb;
+  if (fb > tc_max_fb(L->nc)) fb = tc_max_fb(L->nc);
   L->fb = fb;
   // the items of one chunk run side by side, so a chunk's geometry (16 KB per scatterer at
   // U = 2) should stay resident in L2: 16,384 scatterers by default
@@ -571,7 +595,7 @@ void tc_layout(const FsgProbe* probe, const FsgPhantom* ph, int n_ph, int n_tx, 
   }
   L->n_items = items;
   L->off_partial = o;
-  o += tc_a256((size_t)items * fb * kTcTx * kTcE * 8);
+  o += tc_a256((size_t)items * fb * kTcTxChunk * L->nc * kTcE * 8);
   L->off_geo = o;
   o += tc_a256((size_t)tiles * 16 * U * kThreads * 16);
   L->total = o;
@@ -594,7 +618,8 @@ extern "C" int32_t fsg_simus_batched_tc(const FsgProbe* probe, const FsgMedium* 
                                         void* stream_ptr) {
   if (!probe || !medium || !phantoms || !delays) return set_error(FSG_EINVAL, "NULL argument");
   if (n_phantoms < 1 || n_phantoms > kMaxPhantoms) return set_error(FSG_EINVAL, "n_phantoms must be in [1, %d]", kMaxPhantoms);
-  if (n_tx < 1 || n_tx > kTcTx) return set_error(FSG_EUNSUPPORTED, "tensor-core sweep supports n_tx <= %d", kTcTx);
+  if (n_tx < 1 || n_tx > kTcMaxTx)
+    return set_error(FSG_EUNSUPPORTED, "tensor-core sweep supports n_tx <= %d", kTcMaxTx);
   if (probe->n_elements < 1 || probe->n_elements > kTcE)
     return set_error(FSG_EUNSUPPORTED, "tensor-core sweep supports n_elements <= %d", kTcE);
   if (probe->n_sub < 1 || probe->n_sub > 2) return set_error(FSG_EUNSUPPORTED, "tensor-core sweep supports n_sub <= 2");
@@ -701,6 +726,7 @@ extern "C" int32_t fsg_simus_batched_tc(const FsgProbe* probe, const FsgMedium* 
     A.U = U;
     A.n_tx = n_tx;
     A.fb = L.fb;
+    A.nc = L.nc;
     A.chunk = L.chunk;
     A.src_pos = reinterpret_cast<const float4*>(ws + L.off_src);
     A.rot_e = reinterpret_cast<const float2*>(ws + L.off_rot);
@@ -725,7 +751,7 @@ extern "C" int32_t fsg_simus_batched_tc(const FsgProbe* probe, const FsgMedium* 
     a.n_tx = n_tx;
     a.E = E;
     a.fb = L.fb;
-    a.tx_pad = kTcTx;
+    a.tx_pad = kTcTxChunk * L.nc;
     a.e_pad = kTcE;
     a.apply_pp = 1;  // the tensor-core partials carry rc but not pulse x probe
     a.partial = partial;

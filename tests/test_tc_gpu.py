@@ -92,6 +92,30 @@ def test_tc_vs_plain_at_scale_and_graph():
     np.testing.assert_array_equal(rep, spec)
 
 
+@pytest.mark.parametrize("n_tx", [40, 75])
+def test_tc_more_than_32_transmits_vs_plain(n_tx):
+    """40 and 75 firings: accumulators of 2 and 3 column chunks of 32 transmits (N = 128 and
+    192), with 3 and 1 band frequencies per item."""
+    import fastsimus_gb300 as F
+    from fastsimus_gb300 import workloads as W
+    from fastsimus_gb300.batched import BatchedSimus
+
+    p, m = W.cfg1_probe(), W.cfg1_medium()
+    rng = np.random.default_rng(n_tx)
+    phantoms = [(W.uniform_box(rng, 700, (-10e-3, 10e-3), (5e-3, 30e-3)), rng.standard_normal(700)),
+                (W.uniform_box(rng, 130, (-6e-3, 6e-3), (6e-3, 20e-3)), rng.standard_normal(130))]
+    delays = W.plane_wave_delays(p, m, np.linspace(-16.0, 16.0, n_tx))
+    b = BatchedSimus(phantoms, delays, p, m, backend="tc")
+    res = b.run()
+    assert b.device_status() == 0
+    for (s, r), plan, out in zip(phantoms, b.plans, res):
+        spec = np64(out.spectrum)
+        for t in (0, n_tx // 3, n_tx // 2 + 1, n_tx - 1):
+            ref = np64(F.simus_compute(s, r, delays[t], plan, p, m).spectrum)
+            err = G.rel_l2(spec[:, :, t], ref)
+            assert err < TC_TOL, (t, err)
+
+
 def test_tc_rejects_too_many_transmits():
     from fastsimus_gb300 import workloads as W
     from fastsimus_gb300.batched import BatchedSimus
@@ -99,4 +123,4 @@ def test_tc_rejects_too_many_transmits():
     p, m = W.cfg1_probe(), W.cfg1_medium()
     s, r = W.cfg1_scatterers(100)
     with pytest.raises(NotImplementedError):
-        BatchedSimus([(s, r)], W.plane_wave_delays(p, m, np.linspace(-10, 10, 40)), p, m, backend="tc").run()
+        BatchedSimus([(s, r)], W.plane_wave_delays(p, m, np.linspace(-10, 10, 97)), p, m, backend="tc").run()
