@@ -708,6 +708,33 @@ def run_batched_workload(args):
                          "peak": peak, "unit": "TFLOP/s", "frac": flops / (sweep_ms * 1e-3) / 1e12 / peak,
                          "algorithmic_flops_per_launch": flops},
             "autotune_log": getattr(b, "tune_log", None), "clocks": clocks.summary()}
+    # the same batch on the tensor cores (BF16 hi/lo, 1e-3 accuracy class), checked against the
+    # FP32 spectra above
+    try:
+        ref = [o.clone() for o in b.outs]
+        tcb = BatchedSimus(phantoms, delays, p, m, backend="tc", plans=b.plans)
+        tc_best = tcb.autotune(candidates=[BatchTuning(1, 8192, 1), BatchTuning(1, 16384, 1)], cache=False)
+        tcb.capture()
+        for _ in range(args.warmup):
+            tcb.replay()
+        torch.cuda.synchronize()
+        tms = []
+        for _ in range(args.steps):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            tcb.replay()
+            e.record()
+            torch.cuda.synchronize()
+            tms.append(s.elapsed_time(e))
+        rel = [float(torch.linalg.vector_norm(a - r) / torch.linalg.vector_norm(r)) for a, r in zip(tcb.outs, ref)]
+        tc_ms = float(np.mean(tms))
+        line["paths"] = {"tc": {"frames_per_s": frames / (tc_ms * 1e-3), "ms_per_batch": tc_ms,
+                                "speedup_vs_fp32_batched": step_ms / tc_ms, "tuning": tc_best.__dict__,
+                                "status": tcb.device_status(), "relL2_vs_fp32_max": max(rel),
+                                "relL2_vs_fp32_median": float(np.median(rel))}}
+    except Exception as exc:  # recorded in the line
+        line["paths"] = {"tc": {"error": f"{type(exc).__name__}: {exc}"}}
     return line
 
 

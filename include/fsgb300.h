@@ -183,7 +183,7 @@ size_t fsg_simus_batched_tc_workspace_size(const FsgProbe* probe, const FsgPhant
  * contraction over elements and the receive contraction over scatterers run as complex GEMMs
  * on BF16 hi + lo splits of Green's tiles generated on chip in FP32 (three products, FP32
  * accumulation in TMEM).  Accuracy target relative L2 <= 1e-3 against the FP64 reference
- * (measured ~1e-5).  Limits: n_elements <= 64, n_sub <= 2, n_tx <= 32.
+ * (measured ~1e-5).  Limits: n_elements <= 64, n_sub <= 2, n_tx <= 96.
  * tuning->freqs_per_item (1..7, default 6) sets how many frequencies share one Green's
  * geometry pass.  Every device-side wait is bounded; a wait that gives up records
  * FSG_ETIMEOUT, readable with fsg_simus_batched_tc_status.
