@@ -713,7 +713,7 @@ def run_batched_workload(args):
     try:
         ref = [o.clone() for o in b.outs]
         tcb = BatchedSimus(phantoms, delays, p, m, backend="tc", plans=b.plans)
-        tc_best = tcb.autotune(candidates=[BatchTuning(1, 8192, 1), BatchTuning(1, 16384, 1)], cache=False)
+        tc_best = tcb.autotune(candidates=[BatchTuning(fb, c, 1) for fb in (1, 2) for c in (8192, 16384)], cache=False)
         tcb.capture()
         for _ in range(args.warmup):
             tcb.replay()

@@ -207,8 +207,8 @@ class BatchedSimus:
             self.set_tuning(best)
             return best
         if candidates is None and self.backend == "tc":
-            # band frequencies per item that fit TMEM: 7 up to 32 firings, 3 up to 64, 1 beyond
-            top = 7 if self.n_tx <= 32 else (3 if self.n_tx <= 64 else 1)
+            # band frequencies per item that fit TMEM: 7 up to 32 firings, 3 up to 64, 2 beyond
+            top = 7 if self.n_tx <= 32 else (3 if self.n_tx <= 64 else 2)
             candidates = [BatchTuning(fb, c, 1) for fb in range(max(1, top - 2), top + 1) for c in (8192, 16384)]
         if candidates is None:
             total = sum(int(s.shape[0]) for s, _ in self.phantoms)

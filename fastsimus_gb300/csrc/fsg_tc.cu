@@ -36,9 +36,11 @@ constexpr int kTcT = 64;        // scatterers per tile
 constexpr int kTcE = 64;        // padded elements
 constexpr int kTcTxChunk = 32;  // transmits per column chunk: an accumulator has N = 64 nc columns
 constexpr int kTcMaxTx = 96;    // up to nc = 3 chunks
-constexpr int kTcMaxFb = 7;     // TMEM: N (TX) + N per band frequency <= 512 columns
-// Band frequencies per item that fit TMEM with nc transmit chunks: 7, 3, 1.
-__host__ __device__ constexpr int tc_max_fb(int nc) { return 512 / (64 * nc) - 1; }
+constexpr int kTcMaxFb = 7;     // TMEM: the TX accumulator + N per band frequency <= 512 columns
+// The TX product is formed at most two chunks (128 columns) at a time, so TMEM keeps
+// 64 min(nc, 2) TX columns; band frequencies per item that fit: 7, 3, 2.
+__host__ __device__ constexpr int tc_tx_chunks(int nc) { return nc < 2 ? nc : 2; }
+__host__ __device__ constexpr int tc_max_fb(int nc) { return (512 - 64 * tc_tx_chunks(nc)) / (64 * nc); }
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kWaitTries = 1u << 26;
 
@@ -142,6 +144,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int fb = A.fb, E = A.E, T = A.n_tx;
   const int NC = A.nc, NT = kTcTxChunk * NC, N = 2 * NT;
+  const int TXK = tc_tx_chunks(NC), TXC = 64 * TXK;  // chunks per TX pass, TX TMEM columns
   const TcSmem SL = tc_smem(NC);
   if (tid == 0) {
     tc::mbar_init(&mbar_tx, 1);
@@ -159,7 +162,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
   bool rx_pending = false;
 
   const uint32_t sbase = tc::smem_u32(sm);
-  const uint32_t id_tx = tc::idesc_bf16(128, N, 0, 0);  // A K-major, B K-major
+  const uint32_t id_tx = tc::idesc_bf16(128, TXC, 0, 0);  // A K-major, B K-major (a full pass)
   const uint32_t id_rx = tc::idesc_bf16(128, N, 1, 1);  // A MN-major, B MN-major
   float* X = reinterpret_cast<float*>(sm + SL.x);
 
@@ -195,10 +198,11 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
     C.dk = P.dk;
     C.dalpha = P.dalpha;
 
-    // ---- B_tx for the band: K-major rows n' = (c', t), K = e; value D_c'(e, t) ----
+    // ---- B_tx for the band: K-major rows n' = (chunk, c', t mod 32), K = e; value D_c'(e, t),
+    //      so that each chunk of 32 transmits is 64 contiguous rows ----
     for (int i = tid; i < fb * N * 64; i += kThreads) {
       const int f = i / (N * 64), n = (i >> 6) % N, e = i & 63;
-      const int c = n / NT, t = n % NT;
+      const int c = (n >> 5) & 1, t = kTcTxChunk * (n >> 6) + (n & 31);
       float v = 0.f;
       if (f < nf && e < E && t < T) {
         const float w = A.apod[t * E + e];
@@ -300,62 +304,73 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
         tc::fence_before_sync();
         __syncthreads();
         tc::fence_after_sync();
-        // ---- TX MMAs ----
-        if (tid == 0) {
-          const uint32_t bt = sbase + SL.btx + f * SL.btx_bytes;
-#pragma unroll
-          for (int ks = 0; ks < 4; ++ks) {
-            const uint64_t ah = tc::sdesc(sbase + kOffAtxHi + ks * 256, 128, 1024);
-            const uint64_t al = tc::sdesc(sbase + kOffAtxLo + ks * 256, 128, 1024);
-            const uint64_t bh = tc::sdesc(bt + ks * 256, 128, 1024);
-            const uint64_t bl = tc::sdesc(bt + SL.btx_bytes / 2 + ks * 256, 128, 1024);
-            tc::mma_bf16(tmem, ah, bh, id_tx, ks > 0);
-            tc::mma_bf16(tmem, ah, bl, id_tx, 1);
-            tc::mma_bf16(tmem, al, bh, id_tx, 1);
-          }
-          tc::commit(&mbar_tx);
-          wait0(&mbar_tx, ph_tx);
-        }
-        tc::fence_before_sync();
-        __syncthreads();
-        tc::fence_after_sync();
-        if (s_fail) break;
-        // ---- P = combine(D_tx); write B_rx (MN-major rows n' = (c', t), K = s), one chunk
-        //      of 32 transmits at a time ----
+        // ---- TX MMAs, at most two chunks of 32 transmits per pass (columns [0, 64 chunks)),
+        //      then P = combine(D_tx) -> B_rx (MN-major rows n' = (c', t), K = s) chunk by
+        //      chunk ----
         const int row = 32 * q + lane;  // (c, s) with c = row / 64
-        for (int k = 0; k < NC; ++k) {
-          float v[32];
-          tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + h * NT + 32 * k, v);
-          if (row >= 64) {
-#pragma unroll
-            for (int t = 0; t < 32; ++t) X[(h * 64 + (row - 64)) * kXPitch + t] = v[t];
+        for (int k0 = 0; k0 < NC; k0 += TXK) {
+          const int k1 = min(NC, k0 + TXK);
+          if (k0 > 0) {  // the previous pass's TMEM reads and exchange are done
+            tc::fence_before_sync();
+            __syncthreads();
+            tc::fence_after_sync();
           }
-          __syncthreads();
-          if (row < 64) {
-            // h = 0: Pr = D[0,s][0,t] - D[1,s][1,t];  h = 1: Pi = D[0,s][1,t] + D[1,s][0,t];
-            // times the scatterer's reflectivity
-            const float* x = X + ((1 - h) * 64 + row) * kXPitch;
-            const float rw = rcs[row];
+          if (tid == 0) {
+            const uint32_t bt = sbase + SL.btx + f * SL.btx_bytes + 8192u * k0;  // 64 rows per chunk
+            const uint32_t idp = (k1 - k0 == TXK) ? id_tx : tc::idesc_bf16(128, 64 * (k1 - k0), 0, 0);
 #pragma unroll
-            for (int t = 0; t < 32; ++t) v[t] = rw * (h ? v[t] + x[t] : v[t] - x[t]);
-#pragma unroll
-            for (int c8 = 0; c8 < 4; ++c8) {
-              uint4 hh, ll;
-              tc::split8(v + 8 * c8, hh, ll);
-              const uint32_t o = tc::mnmajor_off(h * NT + 32 * k + 8 * c8, row, N / 8);
-              *reinterpret_cast<uint4*>(sm + SL.brx_hi + o) = hh;
-              *reinterpret_cast<uint4*>(sm + SL.brx_lo + o) = ll;
+            for (int ks = 0; ks < 4; ++ks) {
+              const uint64_t ah = tc::sdesc(sbase + kOffAtxHi + ks * 256, 128, 1024);
+              const uint64_t al = tc::sdesc(sbase + kOffAtxLo + ks * 256, 128, 1024);
+              const uint64_t bh = tc::sdesc(bt + ks * 256, 128, 1024);
+              const uint64_t bl = tc::sdesc(bt + SL.btx_bytes / 2 + ks * 256, 128, 1024);
+              tc::mma_bf16(tmem, ah, bh, idp, ks > 0);
+              tc::mma_bf16(tmem, ah, bl, idp, 1);
+              tc::mma_bf16(tmem, al, bh, idp, 1);
             }
+            tc::commit(&mbar_tx);
+            wait0(&mbar_tx, ph_tx);
           }
-          if (k + 1 < NC) __syncthreads();  // X is reused by the next chunk
+          tc::fence_before_sync();
+          __syncthreads();
+          tc::fence_after_sync();
+          if (s_fail) break;
+          for (int k = k0; k < k1; ++k) {
+            float v[32];
+            // chunk k occupies TX columns 64 (k - k0) + [0, 32) (c' = 0) and + [32, 64) (c' = 1)
+            tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + 64 * (k - k0) + 32 * h, v);
+            if (row >= 64) {
+#pragma unroll
+              for (int t = 0; t < 32; ++t) X[(h * 64 + (row - 64)) * kXPitch + t] = v[t];
+            }
+            __syncthreads();
+            if (row < 64) {
+              // h = 0: Pr = D[0,s][0,t] - D[1,s][1,t];  h = 1: Pi = D[0,s][1,t] + D[1,s][0,t];
+              // times the scatterer's reflectivity
+              const float* x = X + ((1 - h) * 64 + row) * kXPitch;
+              const float rw = rcs[row];
+#pragma unroll
+              for (int t = 0; t < 32; ++t) v[t] = rw * (h ? v[t] + x[t] : v[t] - x[t]);
+#pragma unroll
+              for (int c8 = 0; c8 < 4; ++c8) {
+                uint4 hh, ll;
+                tc::split8(v + 8 * c8, hh, ll);
+                const uint32_t o = tc::mnmajor_off(h * NT + 32 * k + 8 * c8, row, N / 8);
+                *reinterpret_cast<uint4*>(sm + SL.brx_hi + o) = hh;
+                *reinterpret_cast<uint4*>(sm + SL.brx_lo + o) = ll;
+              }
+            }
+            if (k + 1 < k1) __syncthreads();  // X is reused by the next chunk
+          }
         }
+        if (s_fail) break;
         tc::fence_proxy_async_smem();
         tc::fence_before_sync();
         __syncthreads();
         tc::fence_after_sync();
         // ---- RX MMAs into this frequency's accumulator ----
         if (tid == 0) {
-          const uint32_t d = tmem + N + N * f;
+          const uint32_t d = tmem + TXC + N * f;
 #pragma unroll
           for (int ks = 0; ks < 4; ++ks) {
             const uint64_t ah = tc::sdesc(sbase + kOffArxHi + ks * 2 * 2048, 2048, 128);
@@ -389,7 +404,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
       for (int k = 0; k < NC; ++k) {
         float v[32];
         const bool have = !first_tile && f < nf && !fail;
-        if (have) tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + N + N * f + h * NT + 32 * k, v);
+        if (have) tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + TXC + N * f + h * NT + 32 * k, v);
         const int row = 32 * q + lane;  // (c, e)
         if (row >= 64) {
 #pragma unroll
