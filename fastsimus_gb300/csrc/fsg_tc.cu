@@ -5,10 +5,11 @@
 // threads per SM pulls items from an atomic counter.  Per tile of 64 scatterers and frequency f:
 //
 //   generate   Gm[s][e] = mean_u G(s, e, u, f)            (FP32 recurrence, 32 states / thread)
-//   TX  (MMA)  D_tx[(c,s)][(c',t)] = sum_e Gc[s][e] * Dc'[e][t]     M=128 N=64 K=64
-//              with c, c' in {re, im}: rows [Gr; Gi], columns [Dr | Di]
+//   TX  (MMA)  D_tx[(c,s)][(c',t)] = sum_e Gc[s][e] * Dc'[e][t]     M=128 N=64 per chunk K=64
+//              with c, c' in {re, im}: rows [Gr; Gi], columns [Dr | Di] per chunk of 32
+//              transmits (at most two chunks per MMA pass)
 //              P = (D_tx[0,s][0,t] - D_tx[1,s][1,t]) + i (D_tx[0,s][1,t] + D_tx[1,s][0,t])
-//   RX  (MMA)  D_rx[f][(c,e)][(c',t)] += sum_s Gc[s][e] * Qc'[s][t]  M=128 N=64 K=64
+//   RX  (MMA)  D_rx[f][(c,e)][(c',t)] += sum_s Gc[s][e] * Qc'[s][t]  M=128 N=64 nc K=64
 //              with rows [Gr^T; Gi^T] (the same BF16 words as the TX operand) and columns
 //              [Qr | Qi], Q = rc_s P; Y = D_rx[0][0] - D_rx[1][1] + i (D_rx[0][1] + D_rx[1][0]) is
 //              formed once per item, and the reduction multiplies it by pulse x probe.
