@@ -134,7 +134,9 @@ __host__ __device__ inline uint32_t tc_smem_bytes(int fb, int nc) {
   return L.btx + (uint32_t)fb * L.btx_bytes + 1024;
 }
 
-template <int U>
+// kSplitTx: the TX product is formed in passes of two chunks (three chunks, N = 192); else in
+// one pass of all nc chunks.
+template <int U, bool kSplitTx>
 __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__ TcArgs A) {
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ uint64_t mbar_tx, mbar_rx;
@@ -145,7 +147,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int fb = A.fb, E = A.E, T = A.n_tx;
   const int NC = A.nc, NT = kTcTxChunk * NC, N = 2 * NT;
-  const int TXK = tc_tx_chunks(NC), TXC = 64 * TXK;  // chunks per TX pass, TX TMEM columns
+  const int TXK = kSplitTx ? 2 : NC, TXC = 64 * TXK;  // chunks per TX pass, TX TMEM columns
+  const int n_pass = kSplitTx ? (NC + 1) / 2 : 1;
   const TcSmem SL = tc_smem(NC);
   if (tid == 0) {
     tc::mbar_init(&mbar_tx, 1);
@@ -199,11 +202,14 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
     C.dk = P.dk;
     C.dalpha = P.dalpha;
 
-    // ---- B_tx for the band: K-major rows n' = (chunk, c', t mod 32), K = e; value D_c'(e, t),
-    //      so that each chunk of 32 transmits is 64 contiguous rows ----
+    // ---- B_tx for the band: K-major rows n', K = e; value D_c'(e, t).  With split TX passes
+    //      the rows are (chunk, c', t mod 32), so that each chunk of 32 transmits is 64
+    //      contiguous rows; else (c', t). ----
     for (int i = tid; i < fb * N * 64; i += kThreads) {
       const int f = i / (N * 64), n = (i >> 6) % N, e = i & 63;
-      const int c = (n >> 5) & 1, t = kTcTxChunk * (n >> 6) + (n & 31);
+      // chunk-major rows when the TX product is formed in passes; else (c', t) order
+      const int c = kSplitTx ? (n >> 5) & 1 : n / NT;
+      const int t = kSplitTx ? kTcTxChunk * (n >> 6) + (n & 31) : n % NT;
       float v = 0.f;
       if (f < nf && e < E && t < T) {
         const float w = A.apod[t * E + e];
@@ -309,16 +315,16 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
         //      then P = combine(D_tx) -> B_rx (MN-major rows n' = (c', t), K = s) chunk by
         //      chunk ----
         const int row = 32 * q + lane;  // (c, s) with c = row / 64
-        for (int k0 = 0; k0 < NC; k0 += TXK) {
-          const int k1 = min(NC, k0 + TXK);
-          if (k0 > 0) {  // the previous pass's TMEM reads and exchange are done
+        for (int pz = 0; pz < n_pass; ++pz) {
+          const int k0 = pz * TXK, k1 = kSplitTx ? min(NC, k0 + 2) : NC;
+          if (kSplitTx && pz > 0) {  // the previous pass's TMEM reads and exchange are done
             tc::fence_before_sync();
             __syncthreads();
             tc::fence_after_sync();
           }
           if (tid == 0) {
             const uint32_t bt = sbase + SL.btx + f * SL.btx_bytes + 8192u * k0;  // 64 rows per chunk
-            const uint32_t idp = (k1 - k0 == TXK) ? id_tx : tc::idesc_bf16(128, 64 * (k1 - k0), 0, 0);
+            const uint32_t idp = (!kSplitTx || k1 - k0 == TXK) ? id_tx : tc::idesc_bf16(128, 64 * (k1 - k0), 0, 0);
 #pragma unroll
             for (int ks = 0; ks < 4; ++ks) {
               const uint64_t ah = tc::sdesc(sbase + kOffAtxHi + ks * 256, 128, 1024);
@@ -338,8 +344,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
           if (s_fail) break;
           for (int k = k0; k < k1; ++k) {
             float v[32];
-            // chunk k occupies TX columns 64 (k - k0) + [0, 32) (c' = 0) and + [32, 64) (c' = 1)
-            tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + 64 * (k - k0) + 32 * h, v);
+            // split passes: chunk k occupies TX columns 64 (k - k0) + 32 c'; one pass: c' NT + 32 k
+            const int col = kSplitTx ? 64 * (k - k0) + 32 * h : h * NT + 32 * k;
+            tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + col, v);
             if (row >= 64) {
 #pragma unroll
               for (int t = 0; t < 32; ++t) X[(h * 64 + (row - 64)) * kXPitch + t] = v[t];
@@ -541,19 +548,19 @@ cudaError_t launch_tc_geometry(int U, int max_tiles, int sms, const TcArgs& A, c
   return cudaGetLastError();
 }
 
-cudaError_t launch_tc(int U, int grid, const TcArgs& A, cudaStream_t s) {
+template <int U, bool kSplitTx>
+static cudaError_t launch_tc_t(int grid, const TcArgs& A, cudaStream_t s) {
   const uint32_t smem = tc_smem_bytes(A.fb, A.nc);
-  cudaError_t e;
-  if (U == 1) {
-    e = cudaFuncSetAttribute(tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    tc_kernel<1><<<grid, kThreads, smem, s>>>(A);
-  } else {
-    e = cudaFuncSetAttribute(tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    tc_kernel<2><<<grid, kThreads, smem, s>>>(A);
-  }
+  cudaError_t e = cudaFuncSetAttribute(tc_kernel<U, kSplitTx>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  tc_kernel<U, kSplitTx><<<grid, kThreads, smem, s>>>(A);
   return cudaGetLastError();
+}
+
+cudaError_t launch_tc(int U, int grid, const TcArgs& A, cudaStream_t s) {
+  const bool split = tc_tx_chunks(A.nc) < A.nc;
+  if (U == 1) return split ? launch_tc_t<1, true>(grid, A, s) : launch_tc_t<1, false>(grid, A, s);
+  return split ? launch_tc_t<2, true>(grid, A, s) : launch_tc_t<2, false>(grid, A, s);
 }
 
 }  // namespace fsg
