@@ -311,29 +311,19 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
         tc::fence_before_sync();
         __syncthreads();
         tc::fence_after_sync();
-        // ---- TX MMAs, at most two chunks of 32 transmits per pass (columns [0, 64 chunks)),
-        //      then P = combine(D_tx) -> B_rx (MN-major rows n' = (c', t), K = s) chunk by
-        //      chunk ----
-        const int row = 32 * q + lane;  // (c, s) with c = row / 64
-        for (int pz = 0; pz < n_pass; ++pz) {
-          const int k0 = pz * TXK, k1 = kSplitTx ? min(NC, k0 + 2) : NC;
-          if (kSplitTx && pz > 0) {  // the previous pass's TMEM reads and exchange are done
-            tc::fence_before_sync();
-            __syncthreads();
-            tc::fence_after_sync();
-          }
+        if constexpr (!kSplitTx) {
+          // ---- TX MMAs (one pass, N columns) ----
           if (tid == 0) {
-            const uint32_t bt = sbase + SL.btx + f * SL.btx_bytes + 8192u * k0;  // 64 rows per chunk
-            const uint32_t idp = (!kSplitTx || k1 - k0 == TXK) ? id_tx : tc::idesc_bf16(128, 64 * (k1 - k0), 0, 0);
+            const uint32_t bt = sbase + SL.btx + f * SL.btx_bytes;
 #pragma unroll
             for (int ks = 0; ks < 4; ++ks) {
               const uint64_t ah = tc::sdesc(sbase + kOffAtxHi + ks * 256, 128, 1024);
               const uint64_t al = tc::sdesc(sbase + kOffAtxLo + ks * 256, 128, 1024);
               const uint64_t bh = tc::sdesc(bt + ks * 256, 128, 1024);
               const uint64_t bl = tc::sdesc(bt + SL.btx_bytes / 2 + ks * 256, 128, 1024);
-              tc::mma_bf16(tmem, ah, bh, idp, ks > 0);
-              tc::mma_bf16(tmem, ah, bl, idp, 1);
-              tc::mma_bf16(tmem, al, bh, idp, 1);
+              tc::mma_bf16(tmem, ah, bh, id_tx, ks > 0);
+              tc::mma_bf16(tmem, ah, bl, id_tx, 1);
+              tc::mma_bf16(tmem, al, bh, id_tx, 1);
             }
             tc::commit(&mbar_tx);
             wait0(&mbar_tx, ph_tx);
@@ -342,11 +332,12 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
           __syncthreads();
           tc::fence_after_sync();
           if (s_fail) break;
-          for (int k = k0; k < k1; ++k) {
+          // ---- P = combine(D_tx); write B_rx (MN-major rows n' = (c', t), K = s), one chunk
+          //      of 32 transmits at a time ----
+          const int row = 32 * q + lane;  // (c, s) with c = row / 64
+          for (int k = 0; k < NC; ++k) {
             float v[32];
-            // split passes: chunk k occupies TX columns 64 (k - k0) + 32 c'; one pass: c' NT + 32 k
-            const int col = kSplitTx ? 64 * (k - k0) + 32 * h : h * NT + 32 * k;
-            tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + col, v);
+            tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + h * NT + 32 * k, v);
             if (row >= 64) {
 #pragma unroll
               for (int t = 0; t < 32; ++t) X[(h * 64 + (row - 64)) * kXPitch + t] = v[t];
@@ -368,7 +359,68 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
                 *reinterpret_cast<uint4*>(sm + SL.brx_lo + o) = ll;
               }
             }
-            if (k + 1 < k1) __syncthreads();  // X is reused by the next chunk
+            if (k + 1 < NC) __syncthreads();  // X is reused by the next chunk
+          }
+        } else {
+          // ---- TX MMAs, at most two chunks of 32 transmits per pass (columns [0, 64 chunks)),
+          //      then P = combine(D_tx) -> B_rx (MN-major rows n' = (c', t), K = s) chunk by
+          //      chunk ----
+          const int row = 32 * q + lane;  // (c, s) with c = row / 64
+          for (int pz = 0; pz < n_pass; ++pz) {
+            const int k0 = pz * TXK, k1 = kSplitTx ? min(NC, k0 + 2) : NC;
+            if (kSplitTx && pz > 0) {  // the previous pass's TMEM reads and exchange are done
+              tc::fence_before_sync();
+              __syncthreads();
+              tc::fence_after_sync();
+            }
+            if (tid == 0) {
+              const uint32_t bt = sbase + SL.btx + f * SL.btx_bytes + 8192u * k0;  // 64 rows per chunk
+              const uint32_t idp = (!kSplitTx || k1 - k0 == TXK) ? id_tx : tc::idesc_bf16(128, 64 * (k1 - k0), 0, 0);
+#pragma unroll
+              for (int ks = 0; ks < 4; ++ks) {
+                const uint64_t ah = tc::sdesc(sbase + kOffAtxHi + ks * 256, 128, 1024);
+                const uint64_t al = tc::sdesc(sbase + kOffAtxLo + ks * 256, 128, 1024);
+                const uint64_t bh = tc::sdesc(bt + ks * 256, 128, 1024);
+                const uint64_t bl = tc::sdesc(bt + SL.btx_bytes / 2 + ks * 256, 128, 1024);
+                tc::mma_bf16(tmem, ah, bh, idp, ks > 0);
+                tc::mma_bf16(tmem, ah, bl, idp, 1);
+                tc::mma_bf16(tmem, al, bh, idp, 1);
+              }
+              tc::commit(&mbar_tx);
+              wait0(&mbar_tx, ph_tx);
+            }
+            tc::fence_before_sync();
+            __syncthreads();
+            tc::fence_after_sync();
+            if (s_fail) break;
+            for (int k = k0; k < k1; ++k) {
+              float v[32];
+              // split passes: chunk k occupies TX columns 64 (k - k0) + 32 c'; one pass: c' NT + 32 k
+              const int col = kSplitTx ? 64 * (k - k0) + 32 * h : h * NT + 32 * k;
+              tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + col, v);
+              if (row >= 64) {
+#pragma unroll
+                for (int t = 0; t < 32; ++t) X[(h * 64 + (row - 64)) * kXPitch + t] = v[t];
+              }
+              __syncthreads();
+              if (row < 64) {
+                // h = 0: Pr = D[0,s][0,t] - D[1,s][1,t];  h = 1: Pi = D[0,s][1,t] + D[1,s][0,t];
+                // times the scatterer's reflectivity
+                const float* x = X + ((1 - h) * 64 + row) * kXPitch;
+                const float rw = rcs[row];
+#pragma unroll
+                for (int t = 0; t < 32; ++t) v[t] = rw * (h ? v[t] + x[t] : v[t] - x[t]);
+#pragma unroll
+                for (int c8 = 0; c8 < 4; ++c8) {
+                  uint4 hh, ll;
+                  tc::split8(v + 8 * c8, hh, ll);
+                  const uint32_t o = tc::mnmajor_off(h * NT + 32 * k + 8 * c8, row, N / 8);
+                  *reinterpret_cast<uint4*>(sm + SL.brx_hi + o) = hh;
+                  *reinterpret_cast<uint4*>(sm + SL.brx_lo + o) = ll;
+                }
+              }
+              if (k + 1 < k1) __syncthreads();  // X is reused by the next chunk
+            }
           }
         }
         if (s_fail) break;
