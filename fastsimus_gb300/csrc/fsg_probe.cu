@@ -1,6 +1,6 @@
 // Measurement utility: an FP32 FMA throughput probe used to state the FP32 roofline of the
-// plain sweep kernels (the measured peaks cover HBM bandwidth and bf16 tensor rate
-// only).  Each thread runs 8 independent FMA chains; flops = 2 * 8 * iters * threads.
+// plain sweep kernels (the machine's measured-peaks file covers HBM bandwidth and bf16 tensor
+// rate only).  Each thread runs 8 independent FMA chains; flops = 2 * 8 * iters * threads.
 
 #include <cuda_runtime.h>
 
