@@ -458,7 +458,7 @@ def run_gpu_arm(args, rank, world):
 def reference_gpu_leg(args, device, scat, rc, delays, plan, params, medium, flush, our_simus_ms) -> dict:
     """The reference's own CUDA kernel (simus_fused.cu, compiled from its source for sm_103a, stock
     launch shape) on the same frame and GPU: time per sweep (zeroed outputs + kernel, CUDA
-    events, L2 flushed), and its accuracy against this build's sweep on the full frame and
+    events, L2 flushed), and its accuracy against this package's sweep on the full frame and
     against the FP64 oracle on a 512-scatterer sample.  Failure is recorded, not raised."""
     import torch
 

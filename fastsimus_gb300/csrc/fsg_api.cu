@@ -73,9 +73,9 @@ int validate_common(const FsgProbe* probe, const FsgMedium* medium, const FsgFre
   if (!isfinite(plan->freq_start) || !isfinite(plan->freq_step) || !isfinite(plan->seg_length))
     return set_error(FSG_EINVAL, "plan freq_start/freq_step/seg_length must be finite");
   if (probe->n_elements > kThreads)
-    return set_error(FSG_EUNSUPPORTED, "n_elements %d > %d is not supported by this build", probe->n_elements, kThreads);
+    return set_error(FSG_EUNSUPPORTED, "n_elements %d > %d is not supported by this library", probe->n_elements, kThreads);
   if (probe->n_elements * probe->n_sub > 32 * kSrcPerThread)
-    return set_error(FSG_EUNSUPPORTED, "n_elements * n_sub = %d > %d is not supported by this build",
+    return set_error(FSG_EUNSUPPORTED, "n_elements * n_sub = %d > %d is not supported by this library",
                      probe->n_elements * probe->n_sub, 32 * kSrcPerThread);
   if (ffd) {
     // the per-frequency directivity is evaluated as a polynomial valid for |k_f seg / 2| <= 2 pi,
@@ -86,7 +86,7 @@ int validate_common(const FsgProbe* probe, const FsgMedium* medium, const FsgFre
     if (x_max > 2.0 * kPi)
       return set_error(FSG_EUNSUPPORTED,
                        "full_frequency_directivity with sub-elements wider than two wavelengths "
-                       "(k_max seg / 2 = %.3f > 2 pi) is not supported by this build",
+                       "(k_max seg / 2 = %.3f > 2 pi) is not supported by this library",
                        x_max);
   }
   return FSG_OK;
@@ -328,7 +328,7 @@ extern "C" int32_t fsg_simus(const FsgProbe* probe, const FsgMedium* medium, con
                              size_t workspace_bytes, void* stream_ptr) {
   int st = validate_common(probe, medium, plan, ffd);
   if (st != FSG_OK) return st;
-  if (probe->n_sub > 4) return set_error(FSG_EUNSUPPORTED, "n_sub = %d > 4 is not supported by this build", probe->n_sub);
+  if (probe->n_sub > 4) return set_error(FSG_EUNSUPPORTED, "n_sub = %d > 4 is not supported by this library", probe->n_sub);
   if (n_scat < 0) return set_error(FSG_EINVAL, "n_scat must be >= 0");
   if (n_scat > 0 && (!scat_xz || !rc)) return set_error(FSG_EINVAL, "scatterer and rc pointers must be non-NULL");
   if (!delays) return set_error(FSG_EINVAL, "delays pointer must be non-NULL");

@@ -31,7 +31,7 @@ typedef enum FsgStatus {
   FSG_EINVAL = 1,        /* bad argument (NULL pointer, size out of range, ...) */
   FSG_ECUDA = 2,         /* a CUDA runtime call failed */
   FSG_ETIMEOUT = 3,      /* a bounded device-side wait gave up */
-  FSG_EUNSUPPORTED = 4,  /* valid request this build does not implement */
+  FSG_EUNSUPPORTED = 4,  /* valid request this library does not implement */
   FSG_EWORKSPACE = 5     /* workspace smaller than *_workspace_size() */
 } FsgStatus;
 
@@ -165,7 +165,7 @@ size_t fsg_simus_batched_workspace_size(const FsgProbe* probe, const FsgPhantom*
  * (tests/_picmus_phantom_shared.py:319-367, step body _simus_strategies.py:23-77): the
  * Green's terms of each (scatterer, element, frequency) are generated once and contracted with
  * every transmit.  delays/apod are device [n_tx][n_elements] float64 (apod NULL = ones; NaN
- * delay = element off).  Limits of this build: n_elements <= 128 (probes of 65-128 elements use a
+ * delay = element off).  Limits of this library: n_elements <= 128 (probes of 65-128 elements use a
  * 128-element tile with one frequency per work item), n_tx <= 80, n_phantoms <= 64.
  * Phantom descriptors travel as a kernel parameter, so the call contains no host-to-device
  * copy and can be captured in a CUDA graph.

@@ -2,8 +2,8 @@
 
 TEST INFRASTRUCTURE, NOT PRODUCT CODE.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
 ``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` may import this package, and only
-as the checker or as the timed CPU baseline.  The product path (``fastsimus_gb300``) never
-imports it and has no CPU fallback.
+as the tests' expected results or as the timed CPU baseline.  The product path
+(``fastsimus_gb300``) never imports it and has no CPU fallback.
 
 ``oracle.fastsimus_fp64`` restates, in plain FP64 NumPy, the reference's own CPU path
 (charlesbmi/FastSIMUS ``src/fast_simus``): plan, sweep set-up, the per-frequency step body,

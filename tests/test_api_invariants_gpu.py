@@ -1,5 +1,5 @@
 """API invariants of the reference's simus tests (tests/test_simus.py:253-320, :392-427),
-through this build's GPU path on the reference's P4-2v preset."""
+through this package's GPU path on the reference's P4-2v preset."""
 
 import numpy as np
 import pytest

@@ -1,7 +1,7 @@
 """The reference's own CUDA kernel (``simus_fused.cu``, compiled from its source for sm_103a by
 ``oracle/ref_gpu_build.py``) on the same GPU: its accuracy against the reference's FP64 CPU
-path, beside this build's kernel on identical inputs.  The reference kernel is a baseline, so
-its error is reported and only loosely bounded; this build's bound is the 1e-5 target."""
+path, beside this package's kernel on identical inputs.  The reference kernel is a baseline, so
+its error is reported and only loosely bounded; this package's bound is the 1e-5 target."""
 
 import numpy as np
 import pytest
