@@ -4,7 +4,7 @@
 
 Workload (one "step" = one frame): the 128-element scale configuration -- 200,000 scatterers
 in x in [-19, 19] mm, z in [5, 50] mm with three anechoic disks, 0.5 dB/cm/MHz, one 0-degree
-plane wave -> 128-channel RF (plain fused FP32 simus sweep + cuFFT irfft + gate), plus the RMS
+plane wave -> 128-channel RF (plain fused FP32 simus sweep + this library's irfft + gate), plus the RMS
 pressure field on a 256 x 512 grid over the same box.  Inputs are seeded synthetic data.
 
 The JSON line reports RF frames/s (``value``, inputs resident in HBM, L2 flushed before every
@@ -34,7 +34,12 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-METRIC = "RF frames/s (plain fused FP32 simus sweep + 256x512 pfield per frame)"
+# The headline metric: frames/s and Green's terms/s of the tensor-core and surrogate paths beside
+# the plain FP32 kernel, each at relative L2 <= 1e-3 against FP64.  ``value`` is the plain fused
+# FP32 kernel's frame rate on the 200,000-scatterer frame; the tensor-core and surrogate
+# figures on their own workloads are in ``vs_plain_fp32`` (and in full under ``paths``).
+METRIC = "RF frames/s & Green terms/s: TC/surrogate vs plain FP32 kernel at rel-L2\u22641e-3"
+VALUE_IS = "plain fused FP32 kernel: RF frames/s of the 200,000-scatterer frame (simus + 256x512 pfield)"
 UNIT = "frames/s"
 WORKLOAD = ("cfg2: 128-element linear array (pitch 0.30 mm, width 0.27 mm, fc 5.2 MHz, bw 0.67), "
             "c 1540 m/s, 0.5 dB/cm/MHz, 0-degree plane wave, 200,000 scatterers x in [-19,19] mm, "
@@ -100,9 +105,11 @@ def _oracle_pfield_shard(args):
 
 
 def cpu_frame_time(pool, n_workers, scat, rc, grid_pts, delays, plan, pplan, params, medium, s_sample, g_sample):
-    """Seconds per full frame, extrapolated linearly from a sample of s_sample scatterers and
-    g_sample grid points (the sweep cost is linear in both; plan and irfft are excluded on
-    both arms)."""
+    """Seconds per full frame: the simus sweep of s_sample scatterers and the pfield sweep of
+    g_sample grid points, each scaled linearly to the full frame (the sweeps are linear in the
+    scatterers and in the points), plus the irfft + gate of the frame's spectrum, timed once and
+    not scaled (its size does not depend on the scatterer count).  The plans are excluded on
+    both arms."""
     import oracle.fastsimus_fp64 as O
 
     rng = np.random.default_rng(123)
@@ -113,11 +120,28 @@ def cpu_frame_time(pool, n_workers, scat, rc, grid_pts, delays, plan, pplan, par
     t0 = time.perf_counter()
     parts = pool.map(_oracle_simus_shard, [(scat[i], rc[i], delays, plan, params, medium) for i in s_sh])
     spec = sum(parts) * plan.correction_factor
-    O.irfft_and_threshold(spec, plan, params.n_elements)
     t1 = time.perf_counter()
-    pool.map(_oracle_pfield_shard, [(grid_pts[i], delays, pplan, params, medium) for i in g_sh])
+    O.irfft_and_threshold(spec, plan, params.n_elements)
     t2 = time.perf_counter()
-    return (t1 - t0) * scat.shape[0] / s_sample + (t2 - t1) * grid_pts.shape[0] / g_sample
+    pool.map(_oracle_pfield_shard, [(grid_pts[i], delays, pplan, params, medium) for i in g_sh])
+    t3 = time.perf_counter()
+    return (t1 - t0) * scat.shape[0] / s_sample + (t2 - t1) + (t3 - t2) * grid_pts.shape[0] / g_sample
+
+
+def port_calibration():
+    """The committed single-core timing of the oracle port against the reference's own FP64
+    path on the same inputs (oracle/calibrate_port.py), or None."""
+    p = ROOT / "oracle" / "port_calibration.json"
+    if not p.exists():
+        return None
+    try:
+        d = json.loads(p.read_text())
+    except Exception:
+        return None
+    return {"simus_port_over_reference": d.get("simus_port_over_reference_mean"),
+            "pfield_port_over_reference": d.get("pfield_port_over_reference"), "cpu": d.get("cpu"),
+            "source": "oracle/port_calibration.json (oracle/calibrate_port.py: same inputs and plans, one core, "
+                      "one BLAS thread)"}
 
 
 def make_workload(n_scat=200_000, grid_nx=256, grid_nz=512):
@@ -196,14 +220,17 @@ def run_reference_arm(args, rank, world):
     t = float(np.mean(times))
     val = 1.0 / t
     sample = (f"{s_sample} of {scat.shape[0]} scatterers and {g_sample} of {gpts.shape[0]} grid points per step, "
-              f"sharded over {cores} processes, time scaled linearly to the full frame")
+              f"sharded over {cores} processes, sweep times scaled linearly to the full frame; the irfft + gate "
+              "of the frame timed once, unscaled")
     line = {
-        "metric": METRIC, "value": val, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus, "steps": args.steps,
+        "metric": METRIC, "value": val, "unit": UNIT, "value_is": VALUE_IS, "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "cpu": model, "l2": "n/a (CPU)"},
         "green_terms_per_s": green_terms(plan, pplan, params, scat.shape[0], gpts.shape[0]) * val,
-        "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+                         "port_calibration": port_calibration()},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -275,6 +302,15 @@ def _peaks():
         except Exception:
             pass
     return {}
+
+
+def fp32_theoretical_tflops(device, sm_mhz=None):
+    """SMs x 128 FP32 lanes x 2 flops x the maximum SM clock (or `sm_mhz`)."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    mhz = sm_mhz or _peaks().get("sm_max_mhz") or 2070.0
+    return sms * 128 * 2 * float(mhz) * 1e6 / 1e12
 
 
 def fp32_peak_tflops(device):
@@ -407,7 +443,8 @@ def run_gpu_arm(args, rank, world):
     gt = green_terms(plan, pplan, params, n_scat, n_grid)
     peaks = _peaks()
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "metric": METRIC, "value": value, "unit": UNIT, "value_is": VALUE_IS, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup,
         "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (double-float phase)", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "parallelism": "replicas" if world > 1 else "1 gpu",
@@ -425,6 +462,9 @@ def run_gpu_arm(args, rank, world):
                                        "python bench.py --steps 1 --warmup 1 --no-e2e --scatterers 20000",
                      "peak_source": "measured in-run by fsg_fp32_fma_probe (FP32 FMA chains); MEASURED_PEAKS.json "
                                     "holds only HBM and bf16 tensor peaks",
+                     "peak_theoretical": fp32_theoretical_tflops(device),
+                     "frac_vs_theoretical": achieved / fp32_theoretical_tflops(device),
+                     "theoretical_source": "SMs x 128 FP32 lanes x 2 x max SM clock",
                      "algorithmic_flops_per_launch": flops,
                      "hbm_peak_gbs": peaks.get("hbm_gbs")},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
@@ -444,12 +484,15 @@ def run_gpu_arm(args, rank, world):
         line["cpu_baseline"] = {
             "value": 1.0 / t, "unit": UNIT, "cores": cores, "kind": "port", "cpu": model,
             "sample": f"{args.cpu_scatterers} scatterers + {args.cpu_points} grid points of the frame, sharded over "
-                      f"{cores} processes, scaled linearly to 200,000 scatterers + 131,072 points"}
+                      f"{cores} processes, sweeps scaled linearly to {n_scat} scatterers + {n_grid} points; "
+                      "the irfft + gate of the frame timed once, unscaled",
+            "port_calibration": port_calibration()}
     if not args.no_ref_gpu and world == 1:
         line["reference_gpu_kernel"] = reference_gpu_leg(args, device, scat, rc, delays, plan, params, medium,
                                                          flush, simus_avg)
     if not args.no_paths and world == 1:
         line["paths"] = other_paths(args)
+        line["vs_plain_fp32"] = vs_plain_summary(line["paths"])
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -513,6 +556,32 @@ def reference_gpu_leg(args, device, scat, rc, delays, plan, params, medium, flus
         }
     except Exception as exc:  # recorded in the JSON line
         return {"error": f"{type(exc).__name__}: {exc}"}
+
+
+def vs_plain_summary(paths: dict) -> dict:
+    """The comparison the headline metric names, read from the path measurements: each path's
+    RF frames/s and Green's terms/s beside the plain FP32 kernel on the same workload and GPU,
+    with its error against the FP32 / FP64 results."""
+    out = {}
+    tc = paths.get("tensor_core_cfg4", {})
+    if "paths" in tc:
+        t, pl = tc["paths"].get("tc", {}), tc["paths"].get("plain_fp32_single_transmit", {})
+        out["tensor_core"] = {
+            "workload": "31 plane waves x 262,144 scatterers, 64 elements",
+            "frames_per_s": t.get("frames_per_s"), "green_terms_per_s": t.get("green_terms_per_s"),
+            "plain_fp32_frames_per_s": pl.get("frames_per_s"), "plain_fp32_green_terms_per_s": pl.get("green_terms_per_s"),
+            "speedup_vs_plain": tc.get("speedup_tc_vs_plain"),
+            "relL2_vs_fp64_oracle": t.get("relL2_vs_fp64_oracle"), "relL2_vs_plain_fp32": t.get("relL2_vs_plain_fp32")}
+    elif tc:
+        out["tensor_core"] = tc
+    su = paths.get("surrogate_cfg5", {})
+    if "simus_1M_x75" in su:
+        q = su["simus_1M_x75"]
+        out["surrogate"] = {k: q.get(k) for k in q if k != "breakdown_sample_s"}
+        out["surrogate"]["val_rel_l2"] = su.get("training", {}).get("val_rel_l2")
+    elif su:
+        out["surrogate"] = su
+    return out
 
 
 def other_paths(args) -> dict:
@@ -879,11 +948,15 @@ def run_tc_workload(args):
                                            "ms_per_batch": plain_ms},
         },
         "speedup_tc_vs_plain": plain_ms / tc_ms, "speedup_tc_vs_fp32_batched": fp_ms / tc_ms,
-        "roofline": {"kernel": "tc_kernel", "bound": "tensor", "achieved": tensor_flops / (tc_ms * 1e-3) / 1e12,
-                     "peak": bf16_peak, "unit": "TFLOP/s", "frac": tensor_flops / (tc_ms * 1e-3) / 1e12 / bf16_peak,
+        "roofline": {"kernel": "tc_kernel", "bound": "tensor", "achieved": alg / (tc_ms * 1e-3) / 1e12,
+                     "peak": bf16_peak, "unit": "TFLOP/s", "frac": alg / (tc_ms * 1e-3) / 1e12 / bf16_peak,
+                     "algorithmic_flops_per_launch": alg,
+                     "count": "algorithmic S F (8 E U + 16 E T): the hi/lo split counted once",
+                     "executed_tensor_tflops": tensor_flops / (tc_ms * 1e-3) / 1e12,
+                     "executed_frac": tensor_flops / (tc_ms * 1e-3) / 1e12 / bf16_peak,
+                     "executed_note": "bf16 tensor flops as issued: TX + RX real GEMMs x 3 hi/lo products",
                      "peak_source": "MEASURED_PEAKS.json bf16_tflops (measured)" if "bf16_tflops" in peaks
-                     else "fallback 1890.4", "note": "executed bf16 tensor flops (3 hi/lo products); "
-                     "algorithmic (complex, once) TFLOP/s: " + f"{alg / (tc_ms * 1e-3) / 1e12:.1f}"},
+                     else "fallback 1890.4"},
         "clocks": clocks.summary(),
     }
     return line
@@ -986,8 +1059,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--cpu-scatterers", type=int, default=8192)
-    ap.add_argument("--cpu-points", type=int, default=16384)
+    ap.add_argument("--cpu-scatterers", type=int, default=50_000, help="CPU baseline sample (25%% of the frame)")
+    ap.add_argument("--cpu-points", type=int, default=32_768, help="CPU baseline grid sample (25%% of the grid)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="device timing only (profiling runs)")
     ap.add_argument("--no-ref-gpu", action="store_true",

@@ -1,7 +1,7 @@
 """Device plumbing: tensors in HBM, plan tables on the device, workspaces, streams.
 
-PyTorch is used only for device memory, streams and the cuFFT irfft; all sweep arithmetic runs
-in libfsgb300.so.
+PyTorch is used only for device memory and streams; all arithmetic of the path (sweeps,
+reductions, the spectrum-to-RF epilogue) runs in libfsgb300.so.
 """
 
 from __future__ import annotations

@@ -180,7 +180,7 @@ class BatchedSimus:
         s = torch.cuda.Stream(self.device)
         s.wait_stream(torch.cuda.current_stream(self.device))
         with torch.cuda.stream(s):
-            self.run()  # warm the capture stream (cuFFT plans, attributes)
+            self.run()  # warm the capture stream (kernel attributes, lazy module loading)
         torch.cuda.current_stream(self.device).wait_stream(s)
         torch.cuda.synchronize(self.device)
         with torch.cuda.graph(g):

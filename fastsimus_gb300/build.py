@@ -63,8 +63,20 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
     cc = nvcc()
     flags = ARCH + NVCC_FLAGS + list(extra_flags or [])
 
+    headers = hashlib.sha256()
+    for h in sorted(list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "fsgb300.h"]):
+        headers.update(h.name.encode())
+        headers.update(h.read_bytes())
+    headers.update(" ".join(flags).encode())
+
     def compile_one(src: Path):
+        # an object is reused when its source, every header and the flags are unchanged
         obj = BUILD / (src.stem + ".o")
+        obj_stamp = BUILD / (src.stem + ".digest")
+        h = headers.copy()
+        h.update(src.read_bytes())
+        if not force and obj.exists() and obj_stamp.exists() and obj_stamp.read_text() == h.hexdigest():
+            return obj
         cmd = [cc, *flags, "-c", str(src), "-o", str(obj)]
         if verbose:
             print(" ".join(cmd), flush=True)
@@ -73,6 +85,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
             raise RuntimeError(f"nvcc failed on {src.name}:\n{r.stdout}\n{r.stderr}")
         if verbose and (r.stdout or r.stderr):
             print(r.stdout + r.stderr, flush=True)
+        obj_stamp.write_text(h.hexdigest())
         return obj
 
     srcs = _sources()

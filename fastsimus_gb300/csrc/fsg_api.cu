@@ -307,6 +307,15 @@ static size_t simus_ws_size(const FsgProbe* probe, const FsgFreqPlan* plan, int6
   return need;
 }
 
+// The smallest workspace fsg_simus runs in for this request: the fixed part (tables, status
+// word, partial spectra) plus the geometry cache of one tile, i.e. chunks of one tile each.
+// fsg_simus shrinks its chunks to whatever a smaller-than-default workspace holds above this.
+size_t fsg::simus_min_workspace(const FsgProbe* probe, const FsgFreqPlan* plan, int64_t n_scat, int ffd, int num_sms) {
+  const int E = probe->n_elements, U = probe->n_sub, F = plan->n_freq;
+  SweepConfig c = simus_config(E, U, F, n_scat, num_sms, 0, ffd);  // a zero budget gives one-tile chunks
+  return simus_ws_size(c, E, U, F);
+}
+
 extern "C" size_t fsg_simus_workspace_size(const FsgProbe* probe, const FsgFreqPlan* plan, int64_t n_scat) {
   if (!probe || !plan || probe->n_elements < 1 || probe->n_sub < 1 || plan->n_freq < 1 || n_scat < 0) return 0;
   int sms = 0;

@@ -126,6 +126,9 @@ __global__ void pfield_reduce(const float* __restrict__ partial, int n_bands, in
                               float* __restrict__ out);
 
 int set_error(int code, const char* fmt, ...);
+int device_sm_count(int* out);
+// The smallest workspace in which fsg_simus runs this request (one-tile scatterer chunks).
+size_t simus_min_workspace(const FsgProbe* probe, const FsgFreqPlan* plan, int64_t n_scat, int ffd, int num_sms);
 SweepConst make_sweep_const(const FsgProbe* p, const FsgMedium* m, const FsgFreqPlan* plan, int ffd);
 void convex_geometry(const FsgProbe* p, int* convex, double* apex, double* radius2);
 int check_cuda(cudaError_t err, const char* what);

@@ -9,19 +9,26 @@
 // file-scope device array below.
 //
 // Limits and behaviour:
-//   - The scratch is kNoAllocScratchBytes (16 MiB).  Requests whose fsg_simus workspace would be
-//     larger are rejected with FSG_EINVAL and a message; nothing is launched.  On a 152-SM
-//     GB300 every probe this library supports (n_elements <= 256) fits for any scatterer count
-//     as long as the plan has at most a few thousand frequencies.
+//   - The scratch is kNoAllocScratchBytes (16 MiB).  fsg_simus cuts the scatterers into chunks
+//     whose geometry cache fits the workspace it is given, so the scratch bounds only the fixed
+//     part of a request: the per-frequency tables, the partial spectra (a few slots of
+//     n_freq x n_elements complex64) and the geometry block of one tile.  That is about 12 MiB
+//     for the 128-element, 1,142-frequency probe of the 200,000-scatterer frame, whatever the
+//     scatterer count; a larger scatterer count only means more, smaller chunks.  Requests whose
+//     fixed part does not fit (plans with many thousands of frequencies) are rejected with
+//     FSG_EINVAL and a message; nothing is launched.
 //   - The array is part of this library's device image, so every GPU that loads the library
 //     holds the 16 MiB until the process exits.
 //   - Host code cannot use the array's name as a device address.  The first call on each
 //     device, with that device current, asks the runtime for the address
-//     (cudaGetSymbolAddress) and caches it; make that first call before any stream capture.
+//     (cudaGetSymbolAddress) and caches it for the life of the process; make that first call
+//     before any stream capture.  The cache assumes the device's primary context (the one the
+//     CUDA runtime uses): after cudaDeviceReset, or with another driver-API context current on
+//     the device, the cached address is not valid.
 //   - All calls share the array and it keeps the last call's contents.  Every byte the sweep
 //     reads is written earlier in the same call (tables by the set-up kernel; the partial
-//     spectra are zeroed by the call, then accumulated by the band kernels), so nothing has to
-//     start at zero.
+//     spectra are zeroed by the call, then accumulated by the band kernels; each tile's
+//     geometry block is written before it is read), so nothing has to start at zero.
 //   - Calls whose work overlaps on the GPU (different streams, or different host threads on
 //     one device) race on the shared scratch and corrupt each other's results; serialise them.
 //   - The call allocates nothing: no cudaMalloc, no cudaFree, no allocating library routine.
@@ -67,15 +74,19 @@ extern "C" int32_t fsg_simus_noalloc(const FsgProbe* probe, const FsgMedium* med
                                      const double* apod, int32_t full_frequency_directivity, int32_t out_layout,
                                      void* out, void* stream) {
   if (!probe || !plan) return fsg::set_error(FSG_EINVAL, "probe and plan must be non-NULL");
-  const size_t need = fsg_simus_workspace_size(probe, plan, n_scat);
-  if (need == 0) return fsg::set_error(FSG_EINVAL, "fsg_simus_noalloc: cannot size the scratch for this request");
+  if (probe->n_elements < 1 || probe->n_sub < 1 || plan->n_freq < 1 || n_scat < 0)
+    return fsg::set_error(FSG_EINVAL, "fsg_simus_noalloc: cannot size the scratch for this request");
+  int sms = 0;
+  int st = fsg::device_sm_count(&sms);
+  if (st != FSG_OK) return st;
+  const size_t need = fsg::simus_min_workspace(probe, plan, n_scat, full_frequency_directivity ? 1 : 0, sms);
   if (need > kNoAllocScratchBytes)
     return fsg::set_error(FSG_EINVAL,
-                          "fsg_simus_noalloc: this request needs %zu bytes of scratch but the static scratch holds "
-                          "%zu bytes; use fsg_simus with a caller-provided workspace",
+                          "fsg_simus_noalloc: this request needs at least %zu bytes of scratch but the static scratch "
+                          "holds %zu bytes; use fsg_simus with a caller-provided workspace",
                           need, kNoAllocScratchBytes);
   void* scratch = nullptr;
-  int st = scratch_address(&scratch);
+  st = scratch_address(&scratch);
   if (st != FSG_OK) return st;
   return fsg_simus(probe, medium, plan, scat_xz, rc, n_scat, delays, apod, full_frequency_directivity, out_layout,
                    out, scratch, kNoAllocScratchBytes, stream);

@@ -375,6 +375,3 @@ def cfg5_box(params: TransducerParams) -> Box:
     return Box(x=(-10e-3, 10e-3), z=(5e-3, 30e-3), f=(fc * (1 - bw / 2), fc * (1 + bw / 2)),
                max_angle=16.0 * math.pi / 180.0)
 
-
-def _unused():  # keep ctypes imported for callers that pass byref structs
-    return ctypes

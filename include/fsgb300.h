@@ -249,9 +249,12 @@ int32_t fsg_mlp_adam(float* w, void* w_bf16, const float* grad, float* m1, float
  * (for example a plugin whose host application owns all device memory and passes only input
  * and output buffers).  No counterpart in the reference: it is fsg_simus running on a 16 MiB
  * scratch array held in the library's own device image (see fsg_simus_noalloc_scratch_bytes).
- * Requests needing more scratch fail with FSG_EINVAL.  The first call on a device looks up
- * the array's device address; make it before any stream capture.  All calls share the
- * scratch: calls that overlap on the GPU race, so serialise them.
+ * The scatterers are processed in chunks sized to the scratch, so any scatterer count runs;
+ * a request fails with FSG_EINVAL only when its fixed part (tables, partial spectra of
+ * n_freq x n_elements, one tile of geometry) exceeds the scratch.  The first call on a device
+ * looks up the array's device address in the device's primary context and caches it for the
+ * life of the process; make it before any stream capture.  All calls share the scratch:
+ * calls that overlap on the GPU race, so serialise them.
  */
 int32_t fsg_simus_noalloc(const FsgProbe* probe, const FsgMedium* medium, const FsgFreqPlan* plan,
                           const double* scat_xz, const double* rc, int64_t n_scat,

@@ -31,7 +31,9 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-DEFAULT_REF = Path("/root/reference")
+# The reference tree: FASTSIMUS_REFERENCE_ROOT, or a checkout named "reference" beside this
+# repository.
+DEFAULT_REF = HERE.parent.parent / "reference"
 KERNEL_REL = Path("src/fast_simus/kernels/simus_fused.cu")
 
 # Pinned tuning of the shipped kernel (kernels/cuda_simus.py:50-54).

@@ -13,7 +13,14 @@ GOLDEN = Path(__file__).resolve().parent / "golden"
 
 
 def names(prefix: str = ""):
-    return sorted(p.stem for p in GOLDEN.glob(f"{prefix}*.npz") if p.stem != "plans_known")
+    """Fixtures computed on their own inputs' plans.  The ``*_fullplan`` fixtures, computed on
+    the plan of a larger frame or grid, are listed by ``fullplan_names``."""
+    return sorted(p.stem for p in GOLDEN.glob(f"{prefix}*.npz")
+                  if p.stem != "plans_known" and not p.stem.endswith("_fullplan"))
+
+
+def fullplan_names():
+    return sorted(p.stem for p in GOLDEN.glob("*_fullplan.npz"))
 
 
 def load(name: str) -> SimpleNamespace:

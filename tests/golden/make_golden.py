@@ -101,11 +101,51 @@ def _save(name, params, medium, d):
     print(f"wrote {path.name}: {path.stat().st_size / 1024:.0f} KiB")
 
 
+def cfg2_full_plan_cases(fs_mod):
+    """The 200,000-scatterer, 128-element frame's own plan (1,142 frequencies, k r up to
+    ~2,600 rad): the reference's simus on a random 4,096-scatterer subset of that frame,
+    computed on the plan of the full frame (the sweep is linear in the scatterers, so a subset
+    on the full plan is a valid pin of the full-frame arithmetic), and the reference's pfield
+    on every 8th point of the 256 x 512 grid with the full grid's plan."""
+    from fastsimus_gb300 import workloads as W
+
+    p2, m2 = W.cfg2_probe(), W.cfg2_medium()
+    rp = _ref_params(fs_mod, p2)
+    rm = fs_mod.MediumParams(speed_of_sound=m2.speed_of_sound, attenuation=m2.attenuation)
+    s_full, r_full = W.cfg2_scatterers(200_000)
+    delays = np.zeros(p2.n_elements)
+    plan = fs_mod.simus_precompute(s_full, r_full, delays, rp, rm)
+    idx = np.sort(np.random.default_rng(11).choice(s_full.shape[0], 4096, replace=False))
+    s, r = s_full[idx], r_full[idx]
+    res = fs_mod.simus_compute(s, r, delays, plan, rp, rm, strategy=fs_mod.SimusStrategy.PYTHON)
+    sel = res.spectrum[plan.freq_idx_start: plan.freq_idx_start + plan.selected_freqs.shape[0]]
+    d = dict(kind="simus", scatterers=s, rc=r, delays=delays, ffd=False, apod=np.ones(p2.n_elements),
+             element_splitting=-1, fs=-1.0, subset_of=200_000, subset_index=idx.astype(np.int32),
+             rf=res.rf.astype(np.float32), rf_peak=np.max(np.abs(res.rf)),
+             spectrum_selected=sel.astype(np.complex64))
+    d.update(_plan_dict(plan))
+    _save("simus_cfg2_fullplan", p2, m2, d)
+
+    g_full = W.cfg2_grid()
+    pplan = fs_mod.pfield_precompute(g_full, delays, rp, rm)
+    g = np.ascontiguousarray(g_full[::8, ::8])
+    out = fs_mod.pfield_compute(g, delays, pplan, rp, rm, strategy=fs_mod.PfieldStrategy.VECTORIZED)
+    d = dict(kind="pfield", positions=g, delays=delays, ffd=False, apod=np.ones(p2.n_elements),
+             prms=np.asarray(out, dtype=np.float64), grid_stride=8)
+    d.update(_plan_dict(pplan))
+    _save("pfield_cfg2_fullplan", p2, m2, d)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference-src", default="/root/reference/src")
+    ap.add_argument("--only", choices=["all", "cfg2_fullplan"], default="all",
+                    help="cfg2_fullplan: only the fixtures on the 200,000-scatterer frame's own plans")
     args = ap.parse_args()
     fs_mod = _load_reference(args.reference_src)
+    if args.only == "cfg2_fullplan":
+        cfg2_full_plan_cases(fs_mod)
+        return
 
     from fastsimus_gb300 import workloads as W
     from fastsimus_gb300.params import C5_2v, L11_5v, P4_2v, MediumParams, TransducerParams
@@ -218,6 +258,9 @@ def main():
                                      pp2.n_sub, pp2.seg_length, pp2.correction_factor], dtype=np.float64)
     np.savez_compressed(HERE / "plans_known.npz", **plans)
     print("plans:", {k: v[:1] for k, v in plans.items()})
+
+    # 10. The 200,000-scatterer frame's own simus and pfield plans.
+    cfg2_full_plan_cases(fs_mod)
 
 
 if __name__ == "__main__":

@@ -114,3 +114,26 @@ def test_shared_plan_rule_matches_oracle():
     plo, _ = O.simus_multi_transmit(g.scatterers, g.rc, list(g.delays[:1]), g.params, g.medium)
     np.testing.assert_array_equal(pl.selected_freqs, g.plan_selected_freqs)
     assert pl.n_fft == int(g.plan_n_fft)
+
+
+@pytest.mark.parametrize("name", G.fullplan_names())
+def test_full_frame_plans_match_reference(name):
+    """The plans of the 200,000-scatterer frame and of the 256 x 512 grid, rebuilt here from
+    the full inputs, equal the plans the reference used for the *_fullplan fixtures."""
+    g = G.load(name)
+    if g.kind == "simus":
+        s, r = W.cfg2_scatterers(200_000)
+        np.testing.assert_array_equal(s[g.subset_index], g.scatterers)
+        pl = P.simus_precompute(s, r, g.delays, g.params, g.medium)
+        assert (pl.n_sub, pl.n_freq_full, pl.freq_idx_start, pl.n_fft) == (
+            int(g.plan_n_sub), int(g.plan_n_freq_full), int(g.plan_freq_idx_start), int(g.plan_n_fft))
+        assert pl.selected_freqs.shape[0] == 1142
+    else:
+        grid = W.cfg2_grid()
+        np.testing.assert_array_equal(grid[::8, ::8], g.positions)
+        pl = P.pfield_precompute(grid, g.delays, g.params, g.medium)
+        assert pl.selected_freqs.shape[0] == 274
+    np.testing.assert_array_equal(pl.selected_freqs, g.plan_selected_freqs)
+    np.testing.assert_allclose(pl.pulse_spectrum, g.plan_pulse_spectrum, rtol=0, atol=1e-15)
+    np.testing.assert_allclose(pl.probe_spectrum, g.plan_probe_spectrum, rtol=0, atol=1e-15)
+    assert pl.correction_factor == pytest.approx(float(g.plan_correction_factor), rel=1e-14)

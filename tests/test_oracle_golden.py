@@ -78,3 +78,49 @@ def test_oracle_plans_known_answers():
     row = known["cfg1"]
     assert (pl1.selected_freqs.shape[0], pl1.n_freq_full, pl1.freq_idx_start, pl1.n_fft) == (
         int(row[0]), int(row[6]), int(row[7]), int(row[8]))
+
+
+def _oracle_shard(args):
+    import oracle.fastsimus_fp64 as O_
+
+    s, r, d, plan, p, m = args
+    return O_.simus_spectrum_selected(s, r, d, plan, p, m)
+
+
+def test_oracle_on_full_frame_plan_matches_reference():
+    """The oracle on the 200,000-scatterer frame's own plan (1,142 frequencies, k r up to
+    ~2,600 rad) against the reference on a 4,096-scatterer subset; sharded over processes
+    (the sweep is linear in the scatterers)."""
+    import multiprocessing as mp
+    import os
+
+    from fastsimus_gb300 import workloads as W
+
+    g = G.load("simus_cfg2_fullplan")
+    s_full, r_full = W.cfg2_scatterers(200_000)
+    plan = O.simus_precompute(s_full, r_full, g.delays, g.params, g.medium)
+    _plan_check(g, plan)
+    n = max(1, min(8, len(os.sched_getaffinity(0))))
+    shards = np.array_split(np.arange(g.scatterers.shape[0]), n)
+    # one BLAS thread per worker process (the spawned workers read the environment at start)
+    saved = {v: os.environ.get(v) for v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")}
+    os.environ.update({v: "1" for v in saved})
+    try:
+        with mp.get_context("spawn").Pool(n) as pool:
+            parts = pool.map(_oracle_shard, [(g.scatterers[i], g.rc[i], g.delays, plan, g.params, g.medium)
+                                             for i in shards])
+    finally:
+        for v, old in saved.items():
+            if old is None:
+                os.environ.pop(v, None)
+            else:
+                os.environ[v] = old
+    sel = sum(parts) * plan.correction_factor
+    assert G.rel_l2(sel, g.spectrum_selected) < 2e-7
+    rf, _ = O.irfft_and_threshold(sel, plan, g.params.n_elements)
+    assert G.rel_l2(rf, g.rf) < 2e-7
+
+    gp = G.load("pfield_cfg2_fullplan")
+    pplan = O.pfield_precompute(W.cfg2_grid(), gp.delays, gp.params, gp.medium)
+    out = O.pfield_compute(gp.positions, gp.delays, pplan, gp.params, gp.medium)
+    assert G.rel_l2(out, gp.prms) < 1e-11

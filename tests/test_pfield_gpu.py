@@ -48,3 +48,20 @@ def test_empty_grid_raises():
 
     with pytest.raises(ValueError):
         F.pfield(np.zeros((0, 2)), np.zeros(128), W.cfg2_probe())
+
+
+def test_pfield_full_grid_plan_matches_reference_golden():
+    """The 256 x 512 grid's own plan (274 frequencies): the reference's RMS field on every 8th
+    grid point, computed with the full grid's plan."""
+    import fastsimus_gb300 as F
+    from fastsimus_gb300 import workloads as W
+
+    g = G.load("pfield_cfg2_fullplan")
+    grid = W.cfg2_grid()
+    np.testing.assert_array_equal(grid[::8, ::8], g.positions)
+    plan = F.pfield_precompute(grid, g.delays, g.params, g.medium)
+    np.testing.assert_array_equal(plan.selected_freqs, g.plan_selected_freqs)
+    out = np64(F.pfield_compute(g.positions, g.delays, plan, g.params, g.medium))
+    err = G.rel_l2(out, g.prms)
+    print(f"pfield full-grid plan: relL2 {err:.3e}")
+    assert err < 1e-5

@@ -1,4 +1,4 @@
-"""Spectrum -> RF epilogue (``fsg_irfft_gate``, replacing the cuFFT irfft + gate of
+"""Spectrum -> RF epilogue (``fsg_irfft_gate``, replacing the irfft + gate of
 simus.py:336-367) against NumPy's FP64 irfft and the reference's gate formula."""
 
 import numpy as np

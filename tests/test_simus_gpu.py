@@ -175,3 +175,52 @@ def test_odd_arrays_and_sub_element_counts_vs_oracle(n_elements, splitting, baff
     err = G.rel_l2(got, ref.rf)
     print(f"E={n_elements} U={splitting} baffle={baffle}: relL2 {err:.2e}")
     assert err < PLAIN_TOL
+
+
+def test_full_frame_plan_matches_reference_golden():
+    """The 200,000-scatterer, 128-element frame's own plan: 1,142 frequencies, k r up to
+    ~2,600 rad, 18 frequency bands.  The reference ran on a random 4,096-scatterer subset of
+    the frame with the full frame's plan (linearity makes that a pin of the full-frame
+    arithmetic).  Checked twice: with the default workspace (one scatterer chunk; 256 tiles x
+    18 bands split unevenly over the SMs) and through the C ABI with a workspace sized for 512
+    scatterers, so the call runs nine chunks, the last one partial, each split unevenly."""
+    import fastsimus_gb300 as F
+    from fastsimus_gb300 import _device, _native
+    from fastsimus_gb300 import workloads as W
+
+    g = G.load("simus_cfg2_fullplan")
+    s_full, r_full = W.cfg2_scatterers(200_000)
+    np.testing.assert_array_equal(s_full[g.subset_index], g.scatterers)
+    plan = F.simus_precompute(s_full, r_full, g.delays, g.params, g.medium)
+    np.testing.assert_array_equal(plan.selected_freqs, g.plan_selected_freqs)
+    assert (plan.n_freq_full, plan.freq_idx_start, plan.n_fft) == (
+        int(g.plan_n_freq_full), int(g.plan_freq_idx_start), int(g.plan_n_fft))
+    i0, nf = plan.freq_idx_start, plan.selected_freqs.shape[0]
+    res = F.simus_compute(g.scatterers, g.rc, g.delays, plan, g.params, g.medium)
+    rf_err = G.rel_l2(np64(res.rf), g.rf)
+    sel = np64(res.spectrum)[i0:i0 + nf]
+    sp_err = G.rel_l2(sel, g.spectrum_selected)
+    ph = G.max_phase_err(sel, g.spectrum_selected)
+    print(f"full plan, default workspace: rf relL2 {rf_err:.3e}, spectrum relL2 {sp_err:.3e}, max phase {ph:.3e} rad")
+    assert rf_err < PLAIN_TOL and sp_err < PLAIN_TOL
+
+    lib = _native.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    tabs = _device.plan_tables(plan, dev)
+    probe, med, fplan = _native.make_probe(g.params, plan.n_sub), _native.make_medium(g.medium), tabs.fsg_plan(plan)
+    scat = torch.as_tensor(g.scatterers, device=dev)
+    rc = torch.as_tensor(g.rc, device=dev)
+    d = torch.as_tensor(g.delays, device=dev)
+    n = g.scatterers.shape[0]
+    small = lib.fsg_simus_workspace_size(probe, fplan, 512)
+    assert small < lib.fsg_simus_workspace_size(probe, fplan, n)
+    ws = torch.empty(small, dtype=torch.uint8, device=dev)
+    out = torch.full((nf, g.params.n_elements), float("nan"), dtype=torch.complex64, device=dev)
+    _native.check(lib.fsg_simus(probe, med, fplan, scat.data_ptr(), rc.data_ptr(), n, d.data_ptr(), None, 0,
+                                _native.FSG_OUT_SELECTED_RAW, out.data_ptr(), ws.data_ptr(), ws.numel(),
+                                torch.cuda.current_stream(dev).cuda_stream))
+    torch.cuda.synchronize()
+    chunked = np64(out) * plan.correction_factor
+    err_c = G.rel_l2(chunked, g.spectrum_selected)
+    print(f"full plan, 512-scatterer workspace (chunked): spectrum relL2 {err_c:.3e}")
+    assert err_c < PLAIN_TOL

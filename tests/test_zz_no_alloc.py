@@ -3,8 +3,11 @@
 It exists for callers that cannot allocate device memory (for example a plugin whose host
 application owns all device memory and passes only input and output buffers).  The test
 allocates inputs and outputs itself -- the entry point allocates nothing -- and checks two
-calls in a row against fsg_simus with a caller workspace, at the plain-kernel tolerance.
-This file is collected last so a failure here never hides another test.
+calls in a row against fsg_simus with a caller workspace, at the plain-kernel tolerance, on
+a small frame and on the 200,000-scatterer frame, whose default workspace is larger than the
+static scratch (the call then runs in more, smaller scatterer chunks).  A plan whose fixed part
+does not fit is rejected before anything is launched.  This file is collected last so a failure
+here never hides another test.
 """
 
 import ctypes
@@ -25,18 +28,29 @@ def _rel(a, b):
     return float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
 
 
-def test_noalloc_matches_workspace_entry_point_twice():
-    require_gpu()
+def _frame(which):
     import fastsimus_gb300 as F
-    from fastsimus_gb300 import _device, _native
     from fastsimus_gb300 import workloads as W
+
+    if which == "cfg1_2k":
+        p, m = W.cfg1_probe(), W.cfg1_medium()
+        s, r = W.cfg1_scatterers(2000, seed=4)
+        delays = W.plane_wave_delays(p, m, [7.0])[0]
+    else:  # the 200,000-scatterer, 128-element frame: its default workspace is far above 16 MiB
+        p, m = W.cfg2_probe(), W.cfg2_medium()
+        s, r = W.cfg2_scatterers(200_000)
+        delays = np.zeros(p.n_elements)
+    return p, m, s, r, delays, F.simus_precompute(s, r, delays, p, m)
+
+
+@pytest.mark.parametrize("which", ["cfg1_2k", "cfg2_200k"])
+def test_noalloc_matches_workspace_entry_point_twice(which):
+    require_gpu()
+    from fastsimus_gb300 import _device, _native
 
     lib = _native.load()
     dev = torch.device("cuda", torch.cuda.current_device())
-    p, m = W.cfg1_probe(), W.cfg1_medium()
-    s, r = W.cfg1_scatterers(2000, seed=4)
-    delays = W.plane_wave_delays(p, m, [7.0])[0]
-    plan = F.simus_precompute(s, r, delays, p, m)
+    p, m, s, r, delays, plan = _frame(which)
     tabs = _device.plan_tables(plan, dev)
     probe, med, fplan = _native.make_probe(p, plan.n_sub), _native.make_medium(m), tabs.fsg_plan(plan)
     scat = torch.as_tensor(s, device=dev)
@@ -45,10 +59,14 @@ def test_noalloc_matches_workspace_entry_point_twice():
     stream = torch.cuda.current_stream(dev).cuda_stream
     shape = (plan.n_freq_full, p.n_elements)
 
-    ws = torch.empty(lib.fsg_simus_workspace_size(probe, fplan, s.shape[0]), dtype=torch.uint8, device=dev)
+    ws_bytes = lib.fsg_simus_workspace_size(probe, fplan, s.shape[0])
+    if which == "cfg2_200k":  # the scratch holds fewer scatterers per chunk than the default workspace
+        assert ws_bytes > lib.fsg_simus_noalloc_scratch_bytes()
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
     ref = torch.empty(shape, dtype=torch.complex64, device=dev)
     _native.check(lib.fsg_simus(probe, med, fplan, scat.data_ptr(), rc.data_ptr(), s.shape[0], d.data_ptr(), None,
                                 0, _native.FSG_OUT_FULL_CORRECTED, ref.data_ptr(), ws.data_ptr(), ws.numel(), stream))
+    del ws
     outs = []
     for _ in range(2):
         out = torch.full(shape, float("nan"), dtype=torch.complex64, device=dev)
@@ -77,7 +95,6 @@ def test_noalloc_rejects_requests_beyond_its_scratch():
     fplan = _native.FsgFreqPlan(n_freq=n_freq, n_freq_full=n_freq, freq_idx_start=0, reserved0=0, freq_start=1e6,
                                 freq_step=10.0, seg_length=2.5e-4, correction_factor=1.0,
                                 pulse_spectrum=pulse.data_ptr(), probe_spectrum=probe_s.data_ptr())
-    assert lib.fsg_simus_workspace_size(probe, fplan, 10) > lib.fsg_simus_noalloc_scratch_bytes()
     scat = torch.zeros((10, 2), dtype=torch.float64, device=dev)
     rc = torch.zeros(10, dtype=torch.float64, device=dev)
     d = torch.zeros(256, dtype=torch.float64, device=dev)
