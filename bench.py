@@ -578,7 +578,9 @@ def vs_plain_summary(paths: dict) -> dict:
     if "simus_1M_x75" in su:
         q = su["simus_1M_x75"]
         out["surrogate"] = {k: q.get(k) for k in q if k != "breakdown_sample_s"}
+        out["surrogate"]["workload"] = "1,000,000 scatterers x 75 plane waves over the cfg1 box"
         out["surrogate"]["val_rel_l2"] = su.get("training", {}).get("val_rel_l2")
+        out["surrogate"]["training_frac_of_bf16_peak"] = su.get("roofline", {}).get("frac")
     elif su:
         out["surrogate"] = su
     return out
@@ -603,7 +605,8 @@ def other_paths(args) -> dict:
             r = fn(a)
             keep = ("metric", "value", "unit", "ms_per_step", "green_terms_per_s", "sweep_ms", "roofline", "paths",
                     "speedup_tc_vs_plain", "speedup_tc_vs_fp32_batched", "config", "training",
-                    "field_rel_l2_1M_queries", "per_query_s", "simus_1M_x75", "clocks", "rf2iq_ms", "das_ms",
+                    "field_rel_l2_1M_queries", "per_query_s", "simus_1M_x75", "clocks",
+                    "rf2iq_ms", "das_ms",
                     "das_terms_per_s", "cpu_baseline", "parity_rel_l2_sample")
             out[name] = {k: r[k] for k in keep if k in r}
             if "training" in out[name]:
@@ -963,93 +966,107 @@ def run_tc_workload(args):
 
 
 def run_surrogate_workload(args):
-    """cfg5: Fourier-feature MLP (64 features, 4 x 256 SiLU, BF16 weights) trained on the GPU by
-    the library's own kernels on 2M exact transmit-field samples over the cfg1 box, the band
-    fc (1 +- B/2) and +-16 deg; then used in simus for 1,000,000 scatterers x 75 plane waves with
-    the exact kernel judging every 64-scatterer tile and recomputing tiles above 1e-3.  The
-    simus part runs on a bounded sample of the phantom and is scaled by scatterer count;
-    the exact FP32 batched sweep is timed on the full phantom."""
+    """cfg5: Fourier-feature MLP (64 features, 4 x 256 SiLU, BF16 weights; a head of five
+    carrier amplitudes) trained by the library's tcgen05 kernels on 2M exact transmit-field
+    samples over the cfg1 box, the band fc (1 +- B/2) and +-16 degrees; then used in simus for
+    1,000,000 scatterers x 75 plane waves with the exact kernel judging every (64-scatterer
+    tile, firing) unit and recomputing units above 1e-3, and answering every query outside the
+    network's domain (frequencies outside its band).  The simus part runs on a bounded sample
+    of the phantom and is scaled by scatterer count; the exact FP32 batched sweep is timed on
+    the full phantom."""
     import torch
 
     from fastsimus_gb300 import build
     from fastsimus_gb300 import workloads as W
     from fastsimus_gb300.batched import BatchedSimus, shared_plan
-    from fastsimus_gb300.surrogate import TxFieldSurrogate, cfg5_box, simus_with_surrogate
+    from fastsimus_gb300.surrogate import TxFieldSurrogate, cfg5_box, mlp_flops_per_sample, simus_with_surrogate
 
     build.build()
     device = torch.device("cuda", _env_int("LOCAL_RANK", 0))
     torch.cuda.set_device(device)
     p, m = W.cfg1_probe(), W.cfg1_medium()
-    sur = TxFieldSurrogate(p, m, cfg5_box(p), seed=0)
-    rep = sur.train(n_train=args.sur_train, epochs=args.sur_epochs, batch=4096)
-    # per-query costs: network inference vs exact field
+    box = cfg5_box(p)
+    sur = TxFieldSurrogate(p, m, box, seed=0)
+    with ClockSampler(device.index or 0) as clocks:
+        rep = sur.train(n_train=args.sur_train, steps=args.sur_steps, evals=3)
+    peaks = _peaks()
+    bf16_peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops", 1890.4))
+    # per-query costs: network inference (tcgen05 forward + carriers) vs the exact field kernel
     q = sur.sample_domain(1 << 20, seed=9)
     for _ in range(2):
         sur.predict(q)
-        sur.predict(q, backend="simt")
         sur.exact(q)
     torch.cuda.synchronize()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     ev[0].record()
-    pred = sur.predict(q)  # fused tcgen05 forward pass
+    pred = sur.predict(q)
     ev[1].record()
     ex = sur.exact(q)
     ev[2].record()
-    sur.predict(q, backend="simt")  # the training kernels' forward pass
-    ev[3].record()
     torch.cuda.synchronize()
     t_net_q = ev[0].elapsed_time(ev[1]) * 1e-3 / q.shape[0]
     t_exact_q = ev[1].elapsed_time(ev[2]) * 1e-3 / q.shape[0]
-    t_net_simt_q = ev[2].elapsed_time(ev[3]) * 1e-3 / q.shape[0]
     val_rel = float(torch.linalg.vector_norm(pred - ex) / torch.linalg.vector_norm(ex))
-    # the 1M x 75 use case
+
+    def simus_case(scat, rc, angles_deg):
+        angles = np.deg2rad(angles_deg)
+        delays = W.plane_wave_delays(p, m, angles_deg)
+        plan = shared_plan(scat, rc, list(delays), p, m)
+        sub = np.random.default_rng(2).choice(scat.shape[0], args.sur_sample, replace=False)
+        simus_with_surrogate(sur, scat[sub[:128]], rc[sub[:128]], angles, plan, tol=1e-3, exact_reference=False)
+        res = simus_with_surrogate(sur, scat[sub], rc[sub], angles, plan, tol=1e-3)
+        ex_full = BatchedSimus([(scat, rc)], delays, p, m, plans=[plan], backend="fp32")
+        ex_full.run()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ex_full.run()
+        torch.cuda.synchronize()
+        t_exact_full = time.perf_counter() - t0
+        scale = scat.shape[0] / args.sur_sample
+        t_sur_full = res["t_surrogate_total_s"] * scale
+        frames = len(angles)
+        terms = scat.shape[0] * p.n_elements * plan.n_sub * plan.selected_freqs.shape[0] * frames
+        return {"surrogate_s_scaled": t_sur_full, "exact_fp32_batched_s": t_exact_full,
+                "gain_vs_exact": t_exact_full / t_sur_full, "frames_per_s_surrogate": frames / t_sur_full,
+                "frames_per_s_exact": frames / t_exact_full,
+                "green_terms_per_s_surrogate": terms / t_sur_full, "green_terms_per_s_exact": terms / t_exact_full,
+                "fallback_fraction": res["fallback_fraction"], "network_query_share": res["network_query_share"],
+                "units_in_domain": res["units_in_domain"], "units_failed_judge": res["units_failed_judge"],
+                "unit_rel_err_median": res["unit_rel_err_median"], "unit_rel_err_max": res["unit_rel_err_max"],
+                "rf_rel_l2_vs_exact": res["rf_rel_l2_vs_exact"],
+                "sample_scatterers": args.sur_sample,
+                "breakdown_sample_s": {k: res[k] for k in ("t_network_s", "t_exact_outside_domain_s",
+                                                           "t_judge_fallback_s", "t_rx_s")}}
+
     full_s, full_rc = W.cfg4_scatterers(1_000_000, seed=1)
-    angles = np.deg2rad(np.linspace(-16.0, 16.0, 75))
-    delays = W.plane_wave_delays(p, m, np.rad2deg(angles))
-    plan = shared_plan(full_s, full_rc, list(delays), p, m)
-    sub = np.random.default_rng(2).choice(full_s.shape[0], args.sur_sample, replace=False)
-    simus_with_surrogate(sur, full_s[sub[:128]], full_rc[sub[:128]], angles, plan, tol=1e-3)  # warm-up
-    res = simus_with_surrogate(sur, full_s[sub], full_rc[sub], angles, plan, tol=1e-3)
-    loose = simus_with_surrogate(sur, full_s[sub], full_rc[sub], angles, plan, tol=float("inf"))
-    ex_full = BatchedSimus([(full_s, full_rc)], delays, p, m, plans=[plan], backend="fp32")
-    ex_full.run()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    ex_full.run()
-    torch.cuda.synchronize()
-    t_exact_full = time.perf_counter() - t0
-    scale = full_s.shape[0] / args.sur_sample
-    t_sur_full = res["t_surrogate_total_s"] * scale
-    frames = len(angles)
-    terms = full_s.shape[0] * p.n_elements * plan.n_sub * plan.selected_freqs.shape[0] * frames
+    cfg5 = simus_case(full_s, full_rc, np.linspace(-16.0, 16.0, 75))
     line = {
-        "metric": "RF frames/s & Green terms/s: surrogate (with exact fallback at 1e-3) vs exact FP32 path",
-        "value": frames / t_sur_full, "unit": "frames/s", "n_gpus": 1, "higher_is_better": True,
-        "dtype": "bf16 weights, bf16 hi/lo activations, f32 accumulate (tcgen05 network); f32 exact fallback",
+        "metric": "RF frames/s & Green terms/s: surrogate (exact fallback at 1e-3) vs exact FP32 path",
+        "value": cfg5["frames_per_s_surrogate"], "unit": "frames/s", "n_gpus": 1, "higher_is_better": True,
+        "dtype": "bf16 weights, bf16 hi/lo activations, f32 accumulate (tcgen05 training and inference); "
+                 "f32 exact fallback",
         "data": "synthetic (seeded)",
-        "config": {"workload": "cfg5: cfg1 probe; train 2M samples (x, z, f, theta) over the cfg1 box, "
-                               "fc(1 +- B/2), +-16 deg; use 1,000,000 scatterers x 75 plane waves",
-                   "train_samples": args.sur_train, "epochs": args.sur_epochs,
-                   "simus_sample_scatterers": args.sur_sample, "n_freq": int(plan.selected_freqs.shape[0])},
-        "training": {"seconds": rep["train_s"], "data_seconds": rep["data_s"], "steps": rep["steps"],
-                     "final_train_mse": rep["history"][-1]["train_mse"],
-                     "val_rel_l2": rep["history"][-1]["val_rel_l2"], "history": rep["history"]},
+        "config": {"workload": "cfg5: cfg1 probe; train on 2M samples (x, z, f, theta) over the cfg1 box "
+                               "x [-10, 10] mm, z [5, 30] mm, |theta| <= 16 deg, f in fc(1 +- B/2); use 1,000,000 "
+                               "scatterers x 75 plane waves at [-16, 16] deg",
+                   "train_samples": args.sur_train, "steps": rep["steps"], "batch": rep["batch"],
+                   "carriers": "plane wave, 2 aperture-edge waves, 2 grating lobes"},
+        "training": {k: rep[k] for k in ("train_s", "data_s", "steps", "batch", "ms_per_step", "samples_per_s",
+                                         "algorithmic_tflops", "val_rel_l2")},
         "field_rel_l2_1M_queries": val_rel,
-        "per_query_s": {"network": t_net_q, "network_simt_forward": t_net_simt_q, "exact_kernel": t_exact_q,
-                        "ratio_network_over_exact": t_net_q / t_exact_q,
+        "per_query_s": {"network": t_net_q, "exact_kernel": t_exact_q, "ratio_network_over_exact": t_net_q / t_exact_q,
                         "network_tc_status": sur.tc_status()},
-        "simus_1M_x75": {
-            "surrogate_s_scaled": t_sur_full, "exact_fp32_batched_s": t_exact_full,
-            "gain_vs_exact": t_exact_full / t_sur_full,
-            "fallback_fraction": res["fallback_fraction"], "tile_rel_err_median": res["tile_rel_err_median"],
-            "rf_rel_l2_vs_exact_with_fallback": res["rf_rel_l2_vs_exact"],
-            "rf_rel_l2_vs_exact_network_only": loose["rf_rel_l2_vs_exact"],
-            "network_only_s_scaled": loose["t_surrogate_total_s"] * scale,
-            "green_terms_per_s_surrogate": terms / t_sur_full, "green_terms_per_s_exact": terms / t_exact_full,
-            "frames_per_s_exact": frames / t_exact_full,
-            "breakdown_sample_s": {k: res[k] for k in ("t_network_s", "t_judge_fallback_s", "t_rx_s")},
-        },
+        "simus_1M_x75": cfg5,
+        "clocks": clocks.summary(),
     }
+    line["training"]["history"] = rep["history"]
+    line["roofline"] = {"kernel": "mlp_train (fb + dw + adam per step)", "bound": "tensor",
+                        "achieved": rep["algorithmic_tflops"], "peak": bf16_peak, "unit": "TFLOP/s",
+                        "frac": rep["algorithmic_tflops"] / bf16_peak,
+                        "count": f"3 x {mlp_flops_per_sample(sur.n_out):.0f} flops per training sample (forward, "
+                                 "input and weight gradients; the hi/lo split of the forward activations counted once)",
+                        "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (training is a long loop)"
+                        if "bf16_tflops_sustained" in peaks else "fallback"}
     return line
 
 
@@ -1076,7 +1093,7 @@ def main():
     ap.add_argument("--tc-oracle-scatterers", type=int, default=16384)
     ap.add_argument("--tc-only", action="store_true", help="cfg4 profiling case: only the tensor-core sweep")
     ap.add_argument("--sur-train", type=int, default=2_000_000)
-    ap.add_argument("--sur-epochs", type=int, default=20)
+    ap.add_argument("--sur-steps", type=int, default=60_000)
     ap.add_argument("--sur-sample", type=int, default=1024)
     ap.add_argument("--phantoms", type=int, default=16)
     ap.add_argument("--transmits", type=int, default=75)

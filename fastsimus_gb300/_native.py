@@ -17,7 +17,7 @@ LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libfsgb300.so"
 FSG_OK, FSG_EINVAL, FSG_ECUDA, FSG_ETIMEOUT, FSG_EUNSUPPORTED, FSG_EWORKSPACE = range(6)
 FSG_BAFFLE_SOFT, FSG_BAFFLE_RIGID, FSG_BAFFLE_IMPEDANCE = range(3)
 FSG_OUT_SELECTED_RAW, FSG_OUT_FULL_CORRECTED = range(2)
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 
 class FsgError(RuntimeError):
@@ -52,7 +52,33 @@ class FsgPhantom(ctypes.Structure):
 
 class FsgMlpWeights(ctypes.Structure):
     _fields_ = [("packed", ctypes.c_void_p * 4), ("bias", ctypes.c_void_p * 4), ("w_head", ctypes.c_void_p),
-                ("b_head", ctypes.c_void_p), ("bmat", ctypes.c_void_p)]
+                ("b_head", ctypes.c_void_p), ("bmat", ctypes.c_void_p), ("n_out", ctypes.c_int32),
+                ("reserved0", ctypes.c_int32)]
+
+
+class FsgSurrogateDomain(ctypes.Structure):
+    _fields_ = [("x_lo", ctypes.c_double), ("x_hi", ctypes.c_double), ("z_lo", ctypes.c_double),
+                ("z_hi", ctypes.c_double), ("f_lo", ctypes.c_double), ("f_hi", ctypes.c_double),
+                ("max_angle", ctypes.c_double), ("pitch", ctypes.c_double), ("speed_of_sound", ctypes.c_double),
+                ("n_elements", ctypes.c_int32), ("n_carriers", ctypes.c_int32)]
+
+
+_V4 = ctypes.c_void_p * 4
+
+
+class FsgMlpTrain(ctypes.Structure):
+    _fields_ = [("u", ctypes.c_void_p), ("aux", ctypes.c_void_p), ("n_data", ctypes.c_int64),
+                ("seed", ctypes.c_uint64), ("bmat", ctypes.c_void_p),
+                ("w", _V4), ("m_w", _V4), ("v_w", _V4), ("packed_fwd", _V4), ("packed_bwd", _V4),
+                ("b", _V4), ("m_b", _V4), ("v_b", _V4),
+                ("w_head", ctypes.c_void_p), ("m_w_head", ctypes.c_void_p), ("v_w_head", ctypes.c_void_p),
+                ("b_head", ctypes.c_void_p), ("m_b_head", ctypes.c_void_p), ("v_b_head", ctypes.c_void_p),
+                ("n_out", ctypes.c_int32), ("n_tiles", ctypes.c_int32), ("n_split", ctypes.c_int32),
+                ("total_steps", ctypes.c_int32), ("warmup_steps", ctypes.c_int32),
+                ("lr", ctypes.c_float), ("lr_min", ctypes.c_float), ("beta1", ctypes.c_float),
+                ("beta2", ctypes.c_float), ("eps", ctypes.c_float),
+                ("step", ctypes.c_void_p), ("loss_hist", ctypes.c_void_p), ("loss_hist_len", ctypes.c_int32),
+                ("status", ctypes.c_void_p), ("workspace", ctypes.c_void_p), ("workspace_bytes", ctypes.c_size_t)]
 
 
 class FsgBatchTuning(ctypes.Structure):
@@ -105,13 +131,15 @@ _SIGNATURES = {
                                               ctypes.POINTER(FsgBatchTuning), _P, ctypes.c_size_t, _P]),
     "fsg_txfield": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgMedium), ctypes.c_double,
                                      ctypes.c_double, _P, ctypes.c_int64, _P, _P, ctypes.c_size_t, _P]),
-    "fsg_mlp_gemm": (ctypes.c_int32, [_P, ctypes.c_int64, ctypes.c_int64, _P, ctypes.c_int64, ctypes.c_int64,
-                                      ctypes.c_int32, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
-                                      ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P]),
-    "fsg_mlp_features": (ctypes.c_int32, [_P, _P, _P, ctypes.c_int64, _P]),
-    "fsg_mlp_colsum": (ctypes.c_int32, [_P, ctypes.c_int64, ctypes.c_int32, _P, ctypes.c_int32, _P]),
-    "fsg_mlp_adam": (ctypes.c_int32, [_P, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_float, ctypes.c_float,
-                                      ctypes.c_float, ctypes.c_float, ctypes.c_int32, ctypes.c_float, _P]),
+    "fsg_surrogate_inputs": (ctypes.c_int32, [ctypes.POINTER(FsgSurrogateDomain), _P, ctypes.c_int64, _P,
+                                              ctypes.c_double, _P, _P, _P]),
+    "fsg_surrogate_combine": (ctypes.c_int32, [ctypes.POINTER(FsgSurrogateDomain), _P, ctypes.c_int64, _P,
+                                               ctypes.c_double, _P, _P]),
+    "fsg_mlp_train_workspace_size": (ctypes.c_size_t, [ctypes.c_int32, ctypes.c_int32]),
+    "fsg_mlp_train_n_params": (ctypes.c_int64, [ctypes.c_int32]),
+    "fsg_mlp_train_init": (ctypes.c_int32, [ctypes.POINTER(FsgMlpTrain), _P]),
+    "fsg_mlp_train_steps": (ctypes.c_int32, [ctypes.POINTER(FsgMlpTrain), ctypes.c_int32, _P]),
+    "fsg_mlp_train_gradients": (ctypes.c_int32, [ctypes.POINTER(FsgMlpTrain), _P, _P, _P]),
     "fsg_tc_selftest": (ctypes.c_int32, [_P, _P, _P, ctypes.c_int32, ctypes.c_int32, _P, _P]),
     "fsg_simus_noalloc": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgMedium),
                                            ctypes.POINTER(FsgFreqPlan), _P, _P, ctypes.c_int64, _P, _P, ctypes.c_int32,

@@ -1,18 +1,18 @@
 // Fused tcgen05 forward pass of the transmit-field surrogate network (inference).
 //
 // Network: 64 random Fourier features [sin(2 pi B u), cos(2 pi B u)] of the normalised
-// inputs, four hidden layers of 256 with SiLU, a linear (Re, Im) head (the same network that
-// fsg_mlp_gemm trains).  A persistent CTA takes 128 queries at a time and keeps everything on
+// inputs, four hidden layers of 256 with SiLU, a linear head of n_out <= 10 outputs (the same
+// network that the training kernels of fsg_mlp_train.cu train, with the same SiLU).  A persistent CTA takes 128 queries at a time and keeps everything on
 // chip:
 //   features -> A (shared memory, BF16 hi + lo, K-major core matrices)
 //   per hidden layer: D (TMEM, 128 x 256 FP32) = A_hi W^T + A_lo W^T, two tcgen05.mma
 //   kind::f16 per K step of 16, the layer's BF16 weights streamed through two 32 KB
 //   shared-memory buffers by TMA bulk copies (64 input columns per copy);
 //   epilogue: D + bias -> SiLU -> next layer's A (hi + lo), or, after the last hidden layer,
-//   the 256 -> 2 head on the CUDA cores.
+//   the 256 -> n_out head on the CUDA cores.
 // The weights are BF16 (as in training) and multiply exactly; splitting the activations into
-// hi + lo BF16 keeps them at FP32-class precision (~1e-5 relative), so the result agrees with
-// the FP32-activation training kernel.  Every mbarrier wait is bounded: on timeout the CTA
+// hi + lo BF16 keeps them at FP32-class precision (~1e-5 relative), as in the training forward
+// pass.  Every mbarrier wait is bounded: on timeout the CTA
 // records FSG_ETIMEOUT in the status word, frees its TMEM and returns.
 
 #include <cuda_bf16.h>
@@ -39,9 +39,11 @@ constexpr uint32_t kOffB0 = 2 * kMlpABytes;
 constexpr uint32_t kOffB1 = kOffB0 + kMlpChunkBytes;
 constexpr uint32_t kMlpSmem = kOffB1 + kMlpChunkBytes + 1024;
 constexpr uint32_t kMlpWaitTries = 1u << 26;
+constexpr int kMlpMaxOut = 10;
 
-// SiLU with the fast reciprocal (two MUFU operations); within ~2 ulp of z / (1 + exp(-z)).
-__device__ __forceinline__ float mlp_silu(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
+// SiLU z * sigmoid(z) with the fast exponential and reciprocal, evaluated exactly as the
+// training kernels evaluate it.
+__device__ __forceinline__ float mlp_silu(float z) { return z * __fdividef(1.0f, 1.0f + __expf(-z)); }
 
 // Writes 8 consecutive activations (row r, columns k..k+7) as hi and lo BF16 into the K-major
 // A operand.
@@ -61,13 +63,15 @@ __global__ void __launch_bounds__(256, 1) mlp_tc_forward_kernel(const __grid_con
   __shared__ uint32_t tmem_holder;
   __shared__ int s_fail;
   __shared__ float bmat[64 * 4];
-  __shared__ float whead[2 * kMlpWidth];
+  __shared__ float whead[kMlpMaxOut][kMlpWidth];
   __shared__ float bias_s[4][kMlpWidth];
-  __shared__ float2 hsum[kMlpRows];
+  __shared__ float hsum[kMlpRows][kMlpMaxOut];
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nout = W.n_out;
   for (int i = tid; i < 64 * 4; i += blockDim.x) bmat[i] = W.bmat[i];
-  for (int i = tid; i < 2 * kMlpWidth; i += blockDim.x) whead[i] = W.w_head[i];
+  for (int i = tid; i < kMlpMaxOut * kMlpWidth; i += blockDim.x)
+    whead[i / kMlpWidth][i % kMlpWidth] = (i / kMlpWidth < nout) ? W.w_head[i] : 0.f;
   for (int i = tid; i < 4 * kMlpWidth; i += blockDim.x) bias_s[i / kMlpWidth][i % kMlpWidth] = W.bias[i / kMlpWidth][i % kMlpWidth];
   if (tid == 0) {
     for (int b = 0; b < 2; ++b) {
@@ -138,7 +142,9 @@ __global__ void __launch_bounds__(256, 1) mlp_tc_forward_kernel(const __grid_con
     __syncthreads();
     tc::fence_after_sync();
 
-    float2 head = make_float2(0.f, 0.f);
+    float head[kMlpMaxOut];
+#pragma unroll
+    for (int j = 0; j < kMlpMaxOut; ++j) head[j] = 0.f;
     int64_t chunk0 = tile_iter * kChunksPerTile;  // global index of this layer's first chunk
     for (int layer = 0; layer < 4; ++layer) {
       const int K = layer == 0 ? kMlpFeat : kMlpWidth;
@@ -195,9 +201,11 @@ __global__ void __launch_bounds__(256, 1) mlp_tc_forward_kernel(const __grid_con
           for (int g8 = 0; g8 < 4; ++g8) store_a8(sm, row, col0 + 8 * g8, v + 8 * g8);
         } else {
 #pragma unroll
-          for (int i = 0; i < 32; ++i) {
-            head.x = fmaf(v[i], whead[col0 + i], head.x);
-            head.y = fmaf(v[i], whead[kMlpWidth + col0 + i], head.y);
+          for (int j = 0; j < kMlpMaxOut; ++j) {
+            float acc = head[j];
+#pragma unroll
+            for (int i = 0; i < 32; ++i) acc = fmaf(v[i], whead[j][col0 + i], acc);
+            head[j] = acc;
           }
         }
       }
@@ -208,14 +216,15 @@ __global__ void __launch_bounds__(256, 1) mlp_tc_forward_kernel(const __grid_con
     }
     if (s_fail) break;
     // ---- head: combine the two column halves of each row ----
-    if (chalf == 1) hsum[row] = head;
+    if (chalf == 1) {
+#pragma unroll
+      for (int j = 0; j < kMlpMaxOut; ++j) hsum[row][j] = head[j];
+    }
     __syncthreads();
     if (chalf == 0) {
       const int64_t q = tile * kMlpRows + row;
       if (q < n) {
-        const float2 o = hsum[row];
-        out[2 * q] = head.x + o.x + W.b_head[0];
-        out[2 * q + 1] = head.y + o.y + W.b_head[1];
+        for (int j = 0; j < nout; ++j) out[q * nout + j] = head[j] + hsum[row][j] + W.b_head[j];
       }
     }
     __syncthreads();
@@ -264,6 +273,8 @@ extern "C" int32_t fsg_mlp_tc_forward(const FsgMlpWeights* weights, const float*
   for (int l = 0; l < 4; ++l)
     if (!weights->packed[l] || !weights->bias[l]) return set_error(FSG_EINVAL, "layer %d weights or bias missing", l);
   if (!weights->w_head || !weights->b_head || !weights->bmat) return set_error(FSG_EINVAL, "head or features missing");
+  if (weights->n_out < 1 || weights->n_out > kMlpMaxOut)
+    return set_error(FSG_EUNSUPPORTED, "n_out must be in [1, %d] (got %d)", kMlpMaxOut, weights->n_out);
   if (n == 0) return FSG_OK;
   int dev = 0, sms = 0;
   cudaError_t e = cudaGetDevice(&dev);

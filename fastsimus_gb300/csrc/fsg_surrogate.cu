@@ -1,6 +1,5 @@
 // Transmit-field surrogate support: the exact transmit field at arbitrary (x, z, f, theta)
-// samples, and the hand-written kernels that train and evaluate a Fourier-feature MLP
-// (BF16 weights, FP32 accumulation).
+// samples, and the inputs and outputs of the surrogate network.
 //
 // Exact field (the training target and the judge of the network's error).  For a plane wave
 // of steering angle theta on a linear array, delays tau_e = x_e sin(theta) / c - min_e(...)
@@ -10,11 +9,12 @@
 // -- the quantity inside _pfield_strategies.py:48 before |.|^2, evaluated in closed form (no
 // recurrence: every sample has its own f and theta).
 //
-// MLP: features gamma(v) = [sin(2 pi B v), cos(2 pi B v)] of the normalised inputs (64 random
-// frequencies, B fixed), 4 hidden layers of width 256 with SiLU, a linear (Re, Im) head.
-// One tiled GEMM kernel with fused epilogues (bias + SiLU, SiLU derivative) serves the
-// forward pass, both backward GEMMs and inference; weights are read as BF16 and every product
-// accumulates in FP32.
+// Network inputs and outputs.  The network (trained by fsg_mlp_train.cu, evaluated by
+// fsg_mlp_tc.cu) predicts the complex amplitudes of a few analytic carriers whose phases carry
+// the fast oscillation of the field: the ideal plane wave of the firing, the waves from the
+// two ends of the aperture and the two first grating lobes of the element pitch.  fsg_surrogate_inputs normalises the samples and evaluates the
+// carriers (FP64 phases) for training; fsg_surrogate_combine multiplies the predicted
+// amplitudes back onto the carriers.
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -88,130 +88,89 @@ __global__ void txfield_kernel(const TxFieldArgs a) {
 }
 
 // ------------------------------------------------------------------------------------------
-// Tiled GEMM with fused epilogues: C[m][n] = sum_k A(m, k) * B(k, n)
-//   A(m, k) = A[m * a_sm + k * a_sk] (FP32),  B(k, n) = B[k * b_sk + n * b_sn] (FP32 or BF16)
-// epilogue 0: C = acc (+ bias[n])
-// epilogue 1: Z = acc + bias[n]; C = Z; C2 = silu(Z)        (forward hidden layer)
-// epilogue 2: C = acc * silu'(Zs[m][n])                       (backward through SiLU)
-// 64 x 64 output tile per CTA, 256 threads, 4 x 4 outputs per thread, K staged 16 at a time.
+// Surrogate carriers
 // ------------------------------------------------------------------------------------------
-struct GemmArgs {
-  const float* A;
-  int64_t a_sm, a_sk;
-  const void* B;
-  int64_t b_sk, b_sn;
-  int b_bf16;
-  const float* bias;
-  const float* Zs;  // for epilogue 2, leading dim ldc
-  float* C;
-  float* C2;
-  int64_t ldc;
-  int M, N, K, epi, accumulate;
+constexpr int kMaxCarriers = 5;
+constexpr int kAux = 12;  // floats per training row: carriers c_0..c_4, target y (complex)
+
+struct Carriers {
+  double2 c[kMaxCarriers];
 };
 
-__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
-__device__ __forceinline__ float silu_grad(float z) {
-  const float s = 1.0f / (1.0f + __expf(-z));
-  return s * (1.0f + z * (1.0f - s));
-}
-
-__global__ void __launch_bounds__(256) gemm_kernel(const GemmArgs g) {
-  __shared__ float As[16][65];
-  __shared__ float Bs[16][65];
-  const int tid = threadIdx.x;
-  const int tm = tid / 16, tn = tid % 16;
-  const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
-  float acc[4][4] = {};
-  for (int k0 = 0; k0 < g.K; k0 += 16) {
-    for (int i = tid; i < 16 * 64; i += 256) {
-      // consecutive threads walk the unit-stride dimension of each operand (coalesced loads)
-      int kk, mm;
-      if (g.a_sk == 1) { mm = i / 16; kk = i % 16; } else { kk = i / 64; mm = i % 64; }
-      const int m = m0 + mm, k = k0 + kk;
-      As[kk][mm] = (m < g.M && k < g.K) ? g.A[m * g.a_sm + k * g.a_sk] : 0.f;
-      int kb, nn;
-      if (g.b_sn == 1) { kb = i / 64; nn = i % 64; } else { nn = i / 16; kb = i % 16; }
-      const int n = n0 + nn, kq = k0 + kb;
-      float b = 0.f;
-      if (n < g.N && kq < g.K) {
-        const int64_t o = kq * g.b_sk + n * g.b_sn;
-        b = g.b_bf16 ? __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(g.B)[o])
-                     : reinterpret_cast<const float*>(g.B)[o];
-      }
-      Bs[kb][nn] = b;
-    }
-    __syncthreads();
+// c_0: the plane wave exp(i k (x sin th + z cos th - xmin)); c_1, c_2: the waves from the two
+// ends of the aperture, exp(i k (r_edge + x_edge sin th - xmin)); c_3, c_4: the grating lobes
+// m = -1, +1 of the pitch, exp(i k (x sin th_m + z cos th_m - xmin)) with
+// sin th_m = sin th + m lambda / pitch, zero where |sin th_m| >= 1 (evanescent).  Phases are
+// reduced in cycles in FP64, then sincospi.
+__device__ Carriers surrogate_carriers(const FsgSurrogateDomain& d, double x, double z, double f, double th) {
+  const double st = sin(th), ct = cos(th);
+  const double x0 = -0.5 * (d.n_elements - 1) * d.pitch, x1 = -x0;
+  const double xmin = fmin(x0 * st, x1 * st);
+  const double kc = f / d.speed_of_sound;  // cycles per metre
+  const double lp = d.speed_of_sound / f / d.pitch;  // lambda / pitch
+  double path[kMaxCarriers];
+  bool on[kMaxCarriers];
+  path[0] = x * st + z * ct - xmin;
+  const double xl = x0 - 0.5 * d.pitch, xr = x1 + 0.5 * d.pitch;
+  path[1] = sqrt((x - xl) * (x - xl) + z * z) + xl * st - xmin;
+  path[2] = sqrt((x - xr) * (x - xr) + z * z) + xr * st - xmin;
+  on[0] = on[1] = on[2] = true;
 #pragma unroll
-    for (int kk = 0; kk < 16; ++kk) {
-      float a[4], b[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = As[kk][tm + 16 * i];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tn + 16 * j];
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
-    }
-    __syncthreads();
+  for (int m = 0; m < 2; ++m) {
+    const double sm = st + (m ? lp : -lp);
+    on[3 + m] = fabs(sm) < 1.0;
+    path[3 + m] = x * sm + z * sqrt(fmax(0.0, 1.0 - sm * sm)) - xmin;
   }
+  Carriers out;
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int m = m0 + tm + 16 * i, n = n0 + tn + 16 * j;
-      if (m >= g.M || n >= g.N) continue;
-      float v = acc[i][j];
-      const int64_t o = m * g.ldc + n;
-      if (g.epi == 0) {
-        if (g.bias) v += g.bias[n];
-        g.C[o] = g.accumulate ? g.C[o] + v : v;
-      } else if (g.epi == 1) {
-        v += g.bias[n];
-        g.C[o] = v;
-        g.C2[o] = silu(v);
-      } else {
-        g.C[o] = v * silu_grad(g.Zs[o]);
-      }
-    }
+  for (int j = 0; j < kMaxCarriers; ++j) {
+    const double cyc = kc * path[j];
+    const double fr = cyc - rint(cyc);
+    double s, c;
+    sincospi(2.0 * fr, &s, &c);
+    out.c[j] = (on[j] && j < d.n_carriers) ? make_double2(c, s) : make_double2(0.0, 0.0);
+  }
+  return out;
 }
 
-// Fourier features of normalised inputs u (n x 4): feat[n][j] = sin(2 pi B_j . u), feat[n][64 + j] = cos(...)
-__global__ void fourier_features_kernel(const float* u, const float* Bmat, float* feat, int64_t n) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n * 64) return;
-  const int64_t r = i / 64;
-  const int j = (int)(i % 64);
-  const float t = Bmat[4 * j] * u[4 * r] + Bmat[4 * j + 1] * u[4 * r + 1] + Bmat[4 * j + 2] * u[4 * r + 2] +
-                  Bmat[4 * j + 3] * u[4 * r + 3];
-  float s, c;
-  sincospif(2.0f * t, &s, &c);
-  feat[r * 128 + j] = s;
-  feat[r * 128 + 64 + j] = c;
-}
-
-// column sums: out[n] (+)= sum_m X[m][n]
-__global__ void colsum_kernel(const float* X, int64_t M, int N, float* out, int accumulate) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= N) return;
-  float s = 0.f;
-  for (int64_t m = 0; m < M; ++m) s += X[m * N + n];
-  out[n] = accumulate ? out[n] + s : s;
-}
-
-// Adam on FP32 master weights, BF16 copy for the GEMMs.
-__global__ void adam_kernel(float* w, __nv_bfloat16* w_bf16, const float* grad, float* m1, float* m2, int64_t n,
-                            float lr, float b1, float b2, float eps, float bc1, float bc2, float grad_scale) {
+__global__ void surrogate_inputs_kernel(const FsgSurrogateDomain d, const double* __restrict__ samples, int64_t n,
+                                        const float2* __restrict__ field, double inv_scale, float4* __restrict__ u,
+                                        float* __restrict__ aux) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const float g = grad[i] * grad_scale;
-  const float a = b1 * m1[i] + (1.f - b1) * g;
-  const float b = b2 * m2[i] + (1.f - b2) * g * g;
-  m1[i] = a;
-  m2[i] = b;
-  const float v = w[i] - lr * (a / bc1) / (sqrtf(b / bc2) + eps);
-  w[i] = v;
-  if (w_bf16) w_bf16[i] = __float2bfloat16_rn(v);
+  const double x = samples[4 * i], z = samples[4 * i + 1], f = samples[4 * i + 2], th = samples[4 * i + 3];
+  u[i] = make_float4((float)((2.0 * x - (d.x_lo + d.x_hi)) / (d.x_hi - d.x_lo)),
+                     (float)((2.0 * z - (d.z_lo + d.z_hi)) / (d.z_hi - d.z_lo)),
+                     (float)((2.0 * f - (d.f_lo + d.f_hi)) / (d.f_hi - d.f_lo)), (float)(th / d.max_angle));
+  if (!aux) return;
+  const Carriers c = surrogate_carriers(d, x, z, f, th);
+  float* o = aux + kAux * i;
+#pragma unroll
+  for (int j = 0; j < kMaxCarriers; ++j) {
+    o[2 * j] = (float)c.c[j].x;
+    o[2 * j + 1] = (float)c.c[j].y;
+  }
+  const float2 y = field ? field[i] : make_float2(0.f, 0.f);
+  o[kAux - 2] = (float)(y.x * inv_scale);
+  o[kAux - 1] = (float)(y.y * inv_scale);
+}
+
+__global__ void surrogate_combine_kernel(const FsgSurrogateDomain d, const double* __restrict__ samples, int64_t n,
+                                         const float* __restrict__ net, double scale, float2* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Carriers c =
+      surrogate_carriers(d, samples[4 * i], samples[4 * i + 1], samples[4 * i + 2], samples[4 * i + 3]);
+  const float* o = net + (size_t)i * 2 * d.n_carriers;
+  double re = 0.0, im = 0.0;
+#pragma unroll
+  for (int j = 0; j < kMaxCarriers; ++j) {
+    if (j < d.n_carriers) {
+      re += (double)o[2 * j] * c.c[j].x - (double)o[2 * j + 1] * c.c[j].y;
+      im += (double)o[2 * j] * c.c[j].y + (double)o[2 * j + 1] * c.c[j].x;
+    }
+  }
+  out[i] = make_float2((float)(re * scale), (float)(im * scale));
 }
 
 }  // namespace fsg
@@ -267,39 +226,33 @@ extern "C" int32_t fsg_txfield(const FsgProbe* probe, const FsgMedium* medium, d
   return check_cuda(cudaGetLastError(), "txfield_kernel launch");
 }
 
-extern "C" int32_t fsg_mlp_gemm(const float* A, int64_t a_sm, int64_t a_sk, const void* B, int64_t b_sk, int64_t b_sn,
-                                int32_t b_bf16, const float* bias, const float* Zs, float* C, float* C2, int64_t ldc,
-                                int32_t M, int32_t N, int32_t K, int32_t epilogue, int32_t accumulate, void* stream) {
-  if (!A || !B || !C || M < 0 || N < 0 || K < 0) return set_error(FSG_EINVAL, "bad gemm arguments");
-  if (epilogue == 1 && (!bias || !C2)) return set_error(FSG_EINVAL, "epilogue 1 needs bias and C2");
-  if (epilogue == 2 && !Zs) return set_error(FSG_EINVAL, "epilogue 2 needs Zs");
-  if (M == 0 || N == 0) return FSG_OK;
-  GemmArgs g{A, a_sm, a_sk, B, b_sk, b_sn, b_bf16, bias, Zs, C, C2, ldc, M, N, K, epilogue, accumulate};
-  if ((M + 63) / 64 > 65535) return set_error(FSG_EINVAL, "M too large for one launch");
-  gemm_kernel<<<dim3((N + 63) / 64, (M + 63) / 64), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(g);
-  return check_cuda(cudaGetLastError(), "gemm_kernel launch");
+static int validate_domain(const FsgSurrogateDomain* d) {
+  if (!d) return set_error(FSG_EINVAL, "NULL domain");
+  if (d->n_carriers < 1 || d->n_carriers > kMaxCarriers) return set_error(FSG_EINVAL, "n_carriers must be 1..5");
+  if (!(d->x_hi > d->x_lo) || !(d->z_hi > d->z_lo) || !(d->f_hi > d->f_lo) || !(d->max_angle > 0) ||
+      !(d->pitch > 0) || !(d->speed_of_sound > 0) || d->n_elements < 1)
+    return set_error(FSG_EINVAL, "bad surrogate domain");
+  return FSG_OK;
 }
 
-extern "C" int32_t fsg_mlp_features(const float* u, const float* bmat, float* feat, int64_t n, void* stream) {
-  if (!u || !bmat || !feat || n < 0) return set_error(FSG_EINVAL, "bad feature arguments");
+extern "C" int32_t fsg_surrogate_inputs(const FsgSurrogateDomain* dom, const double* samples, int64_t n,
+                                        const void* field, double inv_scale, float* u, float* aux, void* stream) {
+  int st = validate_domain(dom);
+  if (st != FSG_OK) return st;
+  if (n < 0 || (n > 0 && (!samples || !u))) return set_error(FSG_EINVAL, "bad surrogate input arguments");
   if (n == 0) return FSG_OK;
-  fourier_features_kernel<<<(unsigned)((n * 64 + 255) / 256), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
-      u, bmat, feat, n);
-  return check_cuda(cudaGetLastError(), "fourier_features launch");
+  surrogate_inputs_kernel<<<(unsigned)((n + 255) / 256), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+      *dom, samples, n, static_cast<const float2*>(field), inv_scale, reinterpret_cast<float4*>(u), aux);
+  return check_cuda(cudaGetLastError(), "surrogate_inputs_kernel launch");
 }
 
-extern "C" int32_t fsg_mlp_colsum(const float* X, int64_t M, int32_t N, float* out, int32_t accumulate, void* stream) {
-  if (!X || !out) return set_error(FSG_EINVAL, "bad colsum arguments");
-  colsum_kernel<<<(N + 127) / 128, 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(X, M, N, out, accumulate);
-  return check_cuda(cudaGetLastError(), "colsum launch");
-}
-
-extern "C" int32_t fsg_mlp_adam(float* w, void* w_bf16, const float* grad, float* m1, float* m2, int64_t n, float lr,
-                                float b1, float b2, float eps, int32_t step, float grad_scale, void* stream) {
-  if (!w || !grad || !m1 || !m2 || n < 0 || step < 1) return set_error(FSG_EINVAL, "bad adam arguments");
+extern "C" int32_t fsg_surrogate_combine(const FsgSurrogateDomain* dom, const double* samples, int64_t n,
+                                         const float* net, double scale, void* out, void* stream) {
+  int st = validate_domain(dom);
+  if (st != FSG_OK) return st;
+  if (n < 0 || (n > 0 && (!samples || !net || !out))) return set_error(FSG_EINVAL, "bad surrogate combine arguments");
   if (n == 0) return FSG_OK;
-  const float bc1 = 1.f - powf(b1, (float)step), bc2 = 1.f - powf(b2, (float)step);
-  adam_kernel<<<(unsigned)((n + 255) / 256), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
-      w, static_cast<__nv_bfloat16*>(w_bf16), grad, m1, m2, n, lr, b1, b2, eps, bc1, bc2, grad_scale);
-  return check_cuda(cudaGetLastError(), "adam launch");
+  surrogate_combine_kernel<<<(unsigned)((n + 255) / 256), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+      *dom, samples, n, net, scale, static_cast<float2*>(out));
+  return check_cuda(cudaGetLastError(), "surrogate_combine_kernel launch");
 }

@@ -3,19 +3,30 @@
 The network maps (x, z, f, theta) -- a point, a frequency and a plane-wave steering angle --
 to the complex transmit pressure of the array (the pressure inside the pfield step body,
 _pfield_strategies.py:48, before |.|^2).  Architecture: 64 random Fourier features of the
-normalised inputs, 4 hidden layers of width 256 with SiLU, a linear (Re, Im) head; BF16
-weights, FP32 accumulation.  Training, inference and the gradients all run in libfsgb300's own
-kernels (``fsg_mlp_gemm`` with fused bias/SiLU epilogues, ``fsg_mlp_features``,
-``fsg_mlp_colsum``, ``fsg_mlp_adam``); PyTorch only holds the buffers.
+normalised inputs, 4 hidden layers of width 256 with SiLU, a linear head; BF16 weights, FP32
+accumulation.
 
-The raw field oscillates at the wavelength in space and at 1/delay in frequency, so the
-network learns the envelope  p * exp(-i phi_c),  phi_c = 2 pi f / c (x sin theta + z cos theta
-- min_e x_e sin theta), the phase of the ideal plane wave; ``predict`` multiplies it back.
+The field oscillates at the wavelength in space and at 1/delay in frequency, and beside the
+plane wave of the firing it carries the waves that start at the two ends of the aperture and,
+at the pitch of these arrays (about one wavelength), the first grating lobes.  The head
+therefore predicts the complex amplitudes a_j of five analytic carriers c_j -- the ideal plane
+wave, the two edge waves and the grating lobes m = -1, +1, whose phases are computed exactly
+(FP64) from the geometry -- and the field is  p = scale * sum_j a_j c_j.  What is left to learn
+is a set of slowly varying amplitudes.
 
-In simus the network supplies the transmit field at every (scatterer, frequency, firing); the
-exact kernel ``fsg_txfield`` judges each tile of scatterers on a few of its members and any tile
-whose relative L2 error exceeds the tolerance is recomputed exactly.  ``simus_with_surrogate``
-returns the timings that show what the network gains (or loses) against the exact path.
+Training runs entirely in libfsgb300's tcgen05 kernels (fsg_mlp_train_*): a step gathers its
+rows on the device, runs forward and backward on the tensor cores, reduces the weight
+gradients on the tensor cores and applies Adam, in three launches with no host
+synchronisation; the step counter, learning-rate schedule and loss history are device state,
+so many steps are replayed from one CUDA graph.  Inference is the fused tcgen05 forward pass
+(fsg_mlp_tc_forward) followed by fsg_surrogate_combine.  PyTorch only holds the buffers.
+
+In simus the network supplies the transmit field at every (scatterer, frequency, firing) inside
+its domain; the exact kernel ``fsg_txfield`` judges each (tile of scatterers, firing) on a few
+of its scatterers and recomputes the pairs whose relative L2 error exceeds the tolerance.
+Queries outside the network's domain (points outside the box, steering angles beyond it,
+frequencies outside its band) are computed exactly.  ``simus_with_surrogate`` returns the
+timings that show what the network gains (or loses) against the exact path.
 """
 
 from __future__ import annotations
@@ -30,16 +41,17 @@ import torch
 
 from fastsimus_gb300 import _device, _native
 from fastsimus_gb300.params import MediumParams, TransducerParams
-from fastsimus_gb300.plan import element_positions
 
 HIDDEN = 256
 DEPTH = 4
 N_FOURIER = 64
+TILE_ROWS = 128
+AUX = 12  # floats per training row: five complex carriers and the complex target
 
 
 @dataclass
 class Box:
-    """Domain of the surrogate: x, z ranges (m), band (Hz), max steering angle (rad)."""
+    """Domain of the surrogate: x, z ranges (m), band (Hz), max |steering angle| (rad)."""
 
     x: tuple
     z: tuple
@@ -51,35 +63,53 @@ def _check(st):
     _native.check(st)
 
 
+def mlp_flops_per_sample(n_out: int) -> float:
+    """Forward multiply-adds x 2 of one query: 128 -> 256 -> 256 -> 256 -> 256 -> n_out."""
+    return 2.0 * (2 * N_FOURIER * HIDDEN + (DEPTH - 1) * HIDDEN * HIDDEN + HIDDEN * n_out)
+
+
 class TxFieldSurrogate:
-    def __init__(self, params: TransducerParams, medium: MediumParams, box: Box, *, sigma=(6.0, 6.0, 3.0, 3.0),
-                 seed: int = 0, device: torch.device | None = None, tx_n_wavelengths: float = 1.0):
+    def __init__(self, params: TransducerParams, medium: MediumParams, box: Box, *, n_carriers: int = 5,
+                 sigma: float = 0.5, seed: int = 0, device: torch.device | None = None,
+                 tx_n_wavelengths: float = 1.0):
         if not params.is_linear:
             raise NotImplementedError("the transmit-field surrogate supports linear arrays")
+        if n_carriers not in (1, 2, 3, 4, 5):
+            raise ValueError("n_carriers must be in 1..5")
         self.params, self.medium, self.box = params, medium, box
         self.device = device or _device.require_cuda()
         self.lib = _native.load()
         self.tx_n_wavelengths = tx_n_wavelengths
+        self.n_out = 2 * n_carriers
+        dev = self.device
         g = torch.Generator().manual_seed(seed)
-        sig = torch.tensor(sigma, dtype=torch.float32)
-        self.bmat = (torch.randn(N_FOURIER, 4, generator=g) * sig).to(self.device).contiguous()
-        shapes = [(HIDDEN, 2 * N_FOURIER)] + [(HIDDEN, HIDDEN)] * (DEPTH - 1) + [(2, HIDDEN)]
+        self.bmat = (torch.randn(N_FOURIER, 4, generator=g) * sigma).to(dev).contiguous()
+        # PyTorch's nn.Linear initialisation: U(-1/sqrt(fan_in), 1/sqrt(fan_in)) for weights and biases
+        shapes = [(HIDDEN, 2 * N_FOURIER)] + [(HIDDEN, HIDDEN)] * (DEPTH - 1) + [(self.n_out, HIDDEN)]
         self.W, self.b = [], []
         for fan_out, fan_in in shapes:
-            w = torch.randn(fan_out, fan_in, generator=g) * math.sqrt(2.0 / fan_in)
-            self.W.append(w.to(self.device).contiguous())
-            self.b.append(torch.zeros(fan_out, device=self.device))
-        self.Wb = [w.to(torch.bfloat16).contiguous() for w in self.W]
-        self.m = [torch.zeros_like(p) for p in self.W + self.b]
-        self.v = [torch.zeros_like(p) for p in self.W + self.b]
-        self.step = 0
+            bound = 1.0 / math.sqrt(fan_in)
+            self.W.append(((torch.rand(fan_out, fan_in, generator=g) * 2 - 1) * bound).to(dev).contiguous())
+            self.b.append(((torch.rand(fan_out, generator=g) * 2 - 1) * bound).to(dev).contiguous())
+        self.mW = [torch.zeros_like(w) for w in self.W]
+        self.vW = [torch.zeros_like(w) for w in self.W]
+        self.mb = [torch.zeros_like(b) for b in self.b]
+        self.vb = [torch.zeros_like(b) for b in self.b]
+        self.packed_fwd = [torch.empty(self.lib.fsg_mlp_tc_packed_bytes(w.shape[1]), dtype=torch.uint8, device=dev)
+                           for w in self.W[:DEPTH]]
+        self.packed_bwd = [None] + [torch.empty(HIDDEN * HIDDEN * 2, dtype=torch.uint8, device=dev)
+                                    for _ in range(DEPTH - 1)]
+        self.step_counter = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.scale = 1.0
-        epos, _, _ = element_positions(params.n_elements, params.pitch, params.radius)
-        self.elem_x = torch.as_tensor(epos[:, 0], dtype=torch.float64, device=self.device)
         self.probe = _native.make_probe(params, self._n_sub())
         self.med = _native.make_medium(medium)
-        self.ws = _device.workspace(params.n_elements * self._n_sub() * 16 + params.n_elements * 8 + 1024,
-                                    self.device)
+        self.ws = _device.workspace(params.n_elements * self._n_sub() * 16 + params.n_elements * 8 + 1024, dev)
+        self.domain = _native.FsgSurrogateDomain(
+            x_lo=box.x[0], x_hi=box.x[1], z_lo=box.z[0], z_hi=box.z[1], f_lo=box.f[0], f_hi=box.f[1],
+            max_angle=box.max_angle, pitch=float(params.pitch), speed_of_sound=float(medium.speed_of_sound),
+            n_elements=int(params.n_elements), n_carriers=n_carriers)
+        self._pack()
 
     def _n_sub(self):
         lam_min = self.medium.speed_of_sound / (self.params.freq_center * (1.0 + self.params.bandwidth / 2.0))
@@ -88,7 +118,7 @@ class TxFieldSurrogate:
     def _stream(self):
         return _device.stream_handle(self.device)
 
-    # -- exact field, carrier, normalisation -------------------------------------------------
+    # -- exact field, inputs, domain ------------------------------------------------------------
     def exact(self, samples: torch.Tensor) -> torch.Tensor:
         """Exact complex transmit pressure at samples (n, 4) float64 [x, z, f, theta]."""
         s = samples.to(device=self.device, dtype=torch.float64).contiguous()
@@ -97,23 +127,18 @@ class TxFieldSurrogate:
                                     s.shape[0], out.data_ptr(), self.ws.data_ptr(), self.ws.numel(), self._stream()))
         return out
 
-    def carrier(self, samples: torch.Tensor) -> torch.Tensor:
-        x, z, f, th = samples.unbind(-1)
-        st = torch.sin(th)
-        xmin = torch.minimum(self.elem_x.min() * st, self.elem_x.max() * st)
-        cyc = f / self.medium.speed_of_sound * (x * st + z * torch.cos(th) - xmin)
-        cyc = cyc - torch.round(cyc)
-        ph = (2 * math.pi) * cyc
-        return torch.polar(torch.ones_like(ph), ph).to(torch.complex64)
-
-    def normalise(self, samples: torch.Tensor) -> torch.Tensor:
-        b = self.box
-        x, z, f, th = samples.unbind(-1)
-        u = torch.stack([(2 * x - (b.x[0] + b.x[1])) / (b.x[1] - b.x[0]),
-                         (2 * z - (b.z[0] + b.z[1])) / (b.z[1] - b.z[0]),
-                         (2 * f - (b.f[0] + b.f[1])) / (b.f[1] - b.f[0]),
-                         th / b.max_angle], dim=-1)
-        return u.to(torch.float32).contiguous()
+    def inputs(self, samples: torch.Tensor, field: torch.Tensor | None = None, with_aux: bool = True):
+        """Normalised inputs u (n, 4) float32 and, with_aux, the carriers and the scaled target
+        (n, 12) float32, by fsg_surrogate_inputs."""
+        s = samples.to(device=self.device, dtype=torch.float64).contiguous()
+        n = s.shape[0]
+        u = torch.empty(n, 4, dtype=torch.float32, device=self.device)
+        aux = torch.empty(n, AUX, dtype=torch.float32, device=self.device) if with_aux else None
+        _check(self.lib.fsg_surrogate_inputs(self.domain, s.data_ptr(), n,
+                                             field.data_ptr() if field is not None else None, 1.0 / self.scale,
+                                             u.data_ptr(), aux.data_ptr() if aux is not None else None,
+                                             self._stream()))
+        return u, aux
 
     def sample_domain(self, n: int, seed: int) -> torch.Tensor:
         g = torch.Generator(device="cpu").manual_seed(seed)
@@ -123,164 +148,195 @@ class TxFieldSurrogate:
         hi = torch.tensor([b.x[1], b.z[1], b.f[1], b.max_angle], dtype=torch.float64)
         return (lo + r * (hi - lo)).to(self.device)
 
-    # -- network ------------------------------------------------------------------------------
-    def _gemm(self, A, a_sm, a_sk, B, b_sk, b_sn, b_bf16, bias, Zs, C, C2, ldc, M, N, K, epi, acc=0):
-        _check(self.lib.fsg_mlp_gemm(A.data_ptr(), a_sm, a_sk, B.data_ptr(), b_sk, b_sn, b_bf16,
-                                     bias.data_ptr() if bias is not None else None,
-                                     Zs.data_ptr() if Zs is not None else None, C.data_ptr(),
-                                     C2.data_ptr() if C2 is not None else None, ldc, M, N, K, epi, acc,
-                                     self._stream()))
+    def in_domain(self, samples: torch.Tensor) -> torch.Tensor:
+        b = self.box
+        x, z, f, th = samples.unbind(-1)
+        return ((x >= b.x[0]) & (x <= b.x[1]) & (z >= b.z[0]) & (z <= b.z[1]) & (f >= b.f[0]) & (f <= b.f[1])
+                & (th.abs() <= b.max_angle))
 
-    def forward(self, u: torch.Tensor, keep: bool = False):
-        n = u.shape[0]
-        feat = torch.empty(n, 2 * N_FOURIER, device=self.device)
-        _check(self.lib.fsg_mlp_features(u.data_ptr(), self.bmat.data_ptr(), feat.data_ptr(), n, self._stream()))
-        acts, zs = [feat], []
-        x, k = feat, 2 * N_FOURIER
+    # -- network weights ------------------------------------------------------------------------
+    def _pack(self):
+        """The packed BF16 copies of the hidden layers from the FP32 weights (fsg_mlp_train_init
+        also clears the training counters)."""
+        t = self._train_struct(n_tiles=1, n_split=1, n_data=1, u=self.bmat, aux=self.bmat)
+        _check(self.lib.fsg_mlp_train_init(ctypes.byref(t), self._stream()))
+
+    def _weights_struct(self):
+        w = _native.FsgMlpWeights()
         for layer in range(DEPTH):
-            z = torch.empty(n, HIDDEN, device=self.device)
-            a = torch.empty(n, HIDDEN, device=self.device)
-            self._gemm(x, k, 1, self.Wb[layer], 1, k, 1, self.b[layer], None, z, a, HIDDEN, n, HIDDEN, k, 1)
-            zs.append(z)
-            acts.append(a)
-            x, k = a, HIDDEN
-            if not keep:
-                acts[-2] = None
-        out = torch.empty(n, 2, device=self.device)
-        self._gemm(x, HIDDEN, 1, self.Wb[DEPTH], 1, HIDDEN, 1, self.b[DEPTH], None, out, None, 2, n, 2, HIDDEN, 0)
-        return out, (acts, zs)
+            w.packed[layer] = self.packed_fwd[layer].data_ptr()
+            w.bias[layer] = self.b[layer].data_ptr()
+        w.w_head = self.W[DEPTH].data_ptr()
+        w.b_head = self.b[DEPTH].data_ptr()
+        w.bmat = self.bmat.data_ptr()
+        w.n_out = self.n_out
+        return w
 
-    # -- tensor-core inference ------------------------------------------------------------------
-    def _tc_weights(self):
-        """Packed BF16 hidden-layer weights for ``fsg_mlp_tc_forward``; re-packed after every
-        optimiser step."""
-        if getattr(self, "_tc_step", None) != self.step:
-            lib, stream = self.lib, self._stream()
-            self._tc_packed = []
-            for layer in range(DEPTH):
-                k = self.Wb[layer].shape[1]
-                buf = torch.empty(lib.fsg_mlp_tc_packed_bytes(k) // 2, dtype=torch.bfloat16, device=self.device)
-                _check(lib.fsg_mlp_tc_pack(self.Wb[layer].data_ptr(), HIDDEN, k, buf.data_ptr(), stream))
-                self._tc_packed.append(buf)
-            self._tc_head = self.Wb[DEPTH].float().contiguous()  # the head multiplies the same BF16 values
-            w = _native.FsgMlpWeights()
-            for layer in range(DEPTH):
-                w.packed[layer] = self._tc_packed[layer].data_ptr()
-                w.bias[layer] = self.b[layer].data_ptr()
-            w.w_head = self._tc_head.data_ptr()
-            w.b_head = self.b[DEPTH].data_ptr()
-            w.bmat = self.bmat.data_ptr()
-            self._tc_struct = w
-            self._tc_status = torch.zeros(1, dtype=torch.int32, device=self.device)
-            self._tc_step = self.step
-        return self._tc_struct
+    def _train_struct(self, *, n_tiles, n_split, n_data, u, aux, seed=0, total_steps=1, warmup=0, lr=1e-3,
+                      lr_min=0.0, loss_hist=None):
+        need = self.lib.fsg_mlp_train_workspace_size(n_tiles, n_split)
+        if getattr(self, "_train_ws", None) is None or self._train_ws.numel() < need:
+            self._train_ws = _device.workspace(need, self.device)
+        t = _native.FsgMlpTrain()
+        t.u, t.aux, t.n_data, t.seed = u.data_ptr(), aux.data_ptr(), int(n_data), int(seed)
+        t.bmat = self.bmat.data_ptr()
+        for layer in range(DEPTH):
+            t.w[layer] = self.W[layer].data_ptr()
+            t.m_w[layer] = self.mW[layer].data_ptr()
+            t.v_w[layer] = self.vW[layer].data_ptr()
+            t.packed_fwd[layer] = self.packed_fwd[layer].data_ptr()
+            t.packed_bwd[layer] = self.packed_bwd[layer].data_ptr() if self.packed_bwd[layer] is not None else None
+            t.b[layer] = self.b[layer].data_ptr()
+            t.m_b[layer] = self.mb[layer].data_ptr()
+            t.v_b[layer] = self.vb[layer].data_ptr()
+        t.w_head, t.m_w_head, t.v_w_head = (self.W[DEPTH].data_ptr(), self.mW[DEPTH].data_ptr(),
+                                            self.vW[DEPTH].data_ptr())
+        t.b_head, t.m_b_head, t.v_b_head = (self.b[DEPTH].data_ptr(), self.mb[DEPTH].data_ptr(),
+                                            self.vb[DEPTH].data_ptr())
+        t.n_out, t.n_tiles, t.n_split = self.n_out, int(n_tiles), int(n_split)
+        t.total_steps, t.warmup_steps = int(total_steps), int(warmup)
+        t.lr, t.lr_min, t.beta1, t.beta2, t.eps = float(lr), float(lr_min), 0.9, 0.999, 1e-8
+        t.step = self.step_counter.data_ptr()
+        t.loss_hist = loss_hist.data_ptr() if loss_hist is not None else None
+        t.loss_hist_len = int(loss_hist.numel()) if loss_hist is not None else 0
+        t.status = self.status.data_ptr()
+        t.workspace, t.workspace_bytes = self._train_ws.data_ptr(), self._train_ws.numel()
+        return t
 
+    def oracle_params(self):
+        """FP64 copies of the parameters as the kernels multiply them: hidden-layer weights
+        rounded to BF16 (their packed copies), the head and the biases in FP32."""
+        W = [w.to(torch.bfloat16).double().cpu().numpy() for w in self.W[:DEPTH]]
+        W.append(self.W[DEPTH].double().cpu().numpy())
+        return self.bmat.double().cpu().numpy(), W, [b.double().cpu().numpy() for b in self.b]
+
+    # -- training --------------------------------------------------------------------------------
+    def make_dataset(self, n: int, seed: int, scale: float | None = None):
+        """n exact samples over the box: (samples float64, u, aux); sets ``scale`` (the RMS of the
+        field) unless given."""
+        s = self.sample_domain(n, seed)
+        p = self.exact(s)
+        if scale is None:
+            self.scale = float(torch.sqrt((p.abs().double() ** 2).mean()))
+        u, aux = self.inputs(s, p)
+        return s, u, aux, p
+
+    def gradients(self, u: torch.Tensor, aux: torch.Tensor, n_tiles: int = 2, n_split: int = 3, seed: int = 0):
+        """One training step's gradients (no update): (list of weight gradients, list of bias
+        gradients, sampled rows), in the layout of self.W / self.b."""
+        t = self._train_struct(n_tiles=n_tiles, n_split=n_split, n_data=u.shape[0], u=u, aux=aux, seed=seed)
+        n_par = self.lib.fsg_mlp_train_n_params(self.n_out)
+        g = torch.empty(n_par, dtype=torch.float32, device=self.device)
+        rows = torch.empty(n_tiles * TILE_ROWS, dtype=torch.int32, device=self.device)
+        _check(self.lib.fsg_mlp_train_init(ctypes.byref(t), self._stream()))
+        _check(self.lib.fsg_mlp_train_gradients(ctypes.byref(t), g.data_ptr(), rows.data_ptr(), self._stream()))
+        torch.cuda.synchronize(self.device)
+        self._check_status()
+        sizes = [w.numel() for w in self.W[:DEPTH]] + [b.numel() for b in self.b[:DEPTH]] + [
+            self.W[DEPTH].numel(), self.b[DEPTH].numel()]
+        parts = list(torch.split(g, sizes))
+        gW = [parts[i].view_as(self.W[i]) for i in range(DEPTH)] + [parts[2 * DEPTH].view_as(self.W[DEPTH])]
+        gb = [parts[DEPTH + i] for i in range(DEPTH)] + [parts[2 * DEPTH + 1]]
+        return gW, gb, rows.long()
+
+    def _check_status(self):
+        st = int(self.status.item())
+        if st != 0:
+            raise _native.FsgError(st, "a bounded wait in the surrogate kernels gave up")
+
+    def train(self, n_train: int = 2_000_000, steps: int = 30_000, n_tiles: int | None = None, n_split: int = 15,
+              lr: float = 3e-3, lr_min: float = 0.0, warmup_frac: float = 0.05, n_val: int = 65536, seed: int = 0,
+              block: int = 1000, evals: int = 5, log=None) -> dict:
+        """Train on n_train exact samples for `steps` steps of 128 n_tiles rows (default: one
+        tile per SM).  Steps run in CUDA-graph replays of `block` steps; the validation error is
+        measured `evals` times.  Returns the history and the training throughput."""
+        dev = self.device
+        if n_tiles is None:
+            n_tiles = torch.cuda.get_device_properties(dev).multi_processor_count
+        t0 = time.perf_counter()
+        s, u, aux, _ = self.make_dataset(n_train, seed)
+        sv = self.sample_domain(n_val, seed + 1)
+        yv = self.exact(sv)
+        torch.cuda.synchronize(dev)
+        t_data = time.perf_counter() - t0
+        block = max(1, min(block, steps))
+        steps = (steps // block) * block
+        hist_loss = torch.zeros(steps, dtype=torch.float32, device=dev)
+        t = self._train_struct(n_tiles=n_tiles, n_split=n_split, n_data=n_train, u=u, aux=aux, seed=seed,
+                               total_steps=steps, warmup=int(warmup_frac * steps), lr=lr, lr_min=lr_min,
+                               loss_hist=hist_loss)
+        self._tstruct = t  # the captured graph reads it by pointer
+        self.step_counter.zero_()
+        self.status.zero_()
+        _check(self.lib.fsg_mlp_train_init(ctypes.byref(t), self._stream()))
+        # one gradient pass (no update) loads the three kernels before the capture
+        g_tmp = torch.empty(self.lib.fsg_mlp_train_n_params(self.n_out), dtype=torch.float32, device=dev)
+        r_tmp = torch.empty(n_tiles * TILE_ROWS, dtype=torch.int32, device=dev)
+        _check(self.lib.fsg_mlp_train_gradients(ctypes.byref(t), g_tmp.data_ptr(), r_tmp.data_ptr(), self._stream()))
+        torch.cuda.synchronize(dev)
+        del g_tmp, r_tmp
+        graph = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            # the capture records `block` steps; the step counter lives on the device
+            with torch.cuda.graph(graph, stream=side):
+                _check(self.lib.fsg_mlp_train_steps(ctypes.byref(t), block, side.cuda_stream))
+        torch.cuda.current_stream(dev).wait_stream(side)
+        torch.cuda.synchronize(dev)
+        hist, train_ms = [], 0.0
+        eval_at = {max(1, round((i + 1) * (steps // block) / max(1, evals))) for i in range(evals)}
+        for bi in range(steps // block):
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record()
+            graph.replay()
+            ev1.record()
+            torch.cuda.synchronize(dev)
+            train_ms += ev0.elapsed_time(ev1)
+            if (bi + 1) in eval_at:
+                self._check_status()
+                val = self.relative_error(sv, yv)
+                lo = (bi + 1 - 1) * block
+                rec = {"step": (bi + 1) * block, "train_loss": float(hist_loss[lo:(bi + 1) * block].mean()),
+                       "val_rel_l2": val}
+                hist.append(rec)
+                if log:
+                    log(rec)
+        self._check_status()
+        samples = steps * n_tiles * TILE_ROWS
+        flops = 3.0 * mlp_flops_per_sample(self.n_out) * samples
+        return {"history": hist, "train_s": train_ms * 1e-3, "data_s": t_data, "steps": steps,
+                "batch": n_tiles * TILE_ROWS, "samples": n_train, "scale": self.scale,
+                "val_rel_l2": hist[-1]["val_rel_l2"] if hist else None,
+                "ms_per_step": train_ms / steps, "samples_per_s": samples / (train_ms * 1e-3),
+                "algorithmic_tflops": flops / (train_ms * 1e-3) / 1e12,
+                "loss_curve": hist_loss[:: max(1, steps // 200)].cpu().tolist()}
+
+    # -- inference ---------------------------------------------------------------------------------
     def forward_tc(self, u: torch.Tensor) -> torch.Tensor:
-        """The network's output (n x 2) by the fused tcgen05 kernel (inference only)."""
-        w = self._tc_weights()
+        """The network's outputs (n x n_out) by the fused tcgen05 kernel."""
+        w = self._weights_struct()
         u = u.contiguous()
-        out = torch.empty(u.shape[0], 2, device=self.device)
-        _check(self.lib.fsg_mlp_tc_forward(ctypes.byref(w), u.data_ptr(), u.shape[0], out.data_ptr(),
-                                           self._tc_status.data_ptr(), self._stream()))
+        out = torch.empty(u.shape[0], self.n_out, device=self.device)
+        if u.shape[0]:
+            _check(self.lib.fsg_mlp_tc_forward(ctypes.byref(w), u.data_ptr(), u.shape[0], out.data_ptr(),
+                                               self.status.data_ptr(), self._stream()))
         return out
 
     def tc_status(self) -> int:
-        return int(self._tc_status.item()) if hasattr(self, "_tc_status") else 0
-
-    def backward(self, cache, dout: torch.Tensor):
-        acts, zs = cache
-        n = dout.shape[0]
-        gW = [None] * (DEPTH + 1)
-        gb = [None] * (DEPTH + 1)
-        # head
-        gW[DEPTH] = torch.empty(2, HIDDEN, device=self.device)
-        self._gemm(dout, 1, 2, acts[DEPTH], HIDDEN, 1, 0, None, None, gW[DEPTH], None, HIDDEN, 2, HIDDEN, n, 0)
-        gb[DEPTH] = torch.empty(2, device=self.device)
-        _check(self.lib.fsg_mlp_colsum(dout.data_ptr(), n, 2, gb[DEPTH].data_ptr(), 0, self._stream()))
-        dz = torch.empty(n, HIDDEN, device=self.device)
-        self._gemm(dout, 2, 1, self.Wb[DEPTH], HIDDEN, 1, 1, None, zs[DEPTH - 1], dz, None, HIDDEN, n, HIDDEN, 2, 2)
-        for layer in range(DEPTH - 1, -1, -1):
-            a_prev = acts[layer]
-            k = a_prev.shape[1]
-            gW[layer] = torch.empty(HIDDEN, k, device=self.device)
-            self._gemm(dz, 1, HIDDEN, a_prev, k, 1, 0, None, None, gW[layer], None, k, HIDDEN, k, n, 0)
-            gb[layer] = torch.empty(HIDDEN, device=self.device)
-            _check(self.lib.fsg_mlp_colsum(dz.data_ptr(), n, HIDDEN, gb[layer].data_ptr(), 0, self._stream()))
-            if layer > 0:
-                dz_prev = torch.empty(n, HIDDEN, device=self.device)
-                self._gemm(dz, HIDDEN, 1, self.Wb[layer], HIDDEN, 1, 1, None, zs[layer - 1], dz_prev, None, HIDDEN,
-                           n, HIDDEN, HIDDEN, 2)
-                dz = dz_prev
-        return gW, gb
-
-    def loss_and_grads(self, u: torch.Tensor, y: torch.Tensor):
-        out, cache = self.forward(u, keep=True)
-        diff = out - y
-        loss = float((diff * diff).sum()) / (2 * u.shape[0])
-        gW, gb = self.backward(cache, (diff / u.shape[0]).contiguous())
-        return loss, gW, gb
-
-    def adam(self, gW, gb, lr: float, b1=0.9, b2=0.999, eps=1e-8):
-        self.step += 1
-        params = self.W + self.b
-        grads = gW + gb
-        for i, (p, g) in enumerate(zip(params, grads)):
-            wb = self.Wb[i] if i < len(self.W) else None
-            _check(self.lib.fsg_mlp_adam(p.data_ptr(), wb.data_ptr() if wb is not None else None, g.data_ptr(),
-                                         self.m[i].data_ptr(), self.v[i].data_ptr(), p.numel(), lr, b1, b2, eps,
-                                         self.step, 1.0, self._stream()))
-
-    # -- training / inference -----------------------------------------------------------------
-    def make_dataset(self, n: int, seed: int):
-        s = self.sample_domain(n, seed)
-        p = self.exact(s)
-        env = p * torch.conj(self.carrier(s))
-        return s, env
-
-    def train(self, n_train: int = 2_000_000, epochs: int = 20, batch: int = 4096, lr: float = 2e-3,
-              n_val: int = 65536, seed: int = 0, log=None) -> dict:
-        t0 = time.perf_counter()
-        s, env = self.make_dataset(n_train, seed)
-        sv, envv = self.make_dataset(n_val, seed + 1)
-        self.scale = float(torch.sqrt((env.abs() ** 2).mean()))
-        u = self.normalise(s)
-        y = (torch.view_as_real(env) / self.scale).to(torch.float32).contiguous()
-        t_data = time.perf_counter() - t0
-        steps_per_epoch = n_train // batch
-        total = epochs * steps_per_epoch
-        hist = []
-        torch.cuda.synchronize(self.device)
-        t1 = time.perf_counter()
-        g = torch.Generator(device=self.device).manual_seed(seed)
-        it = 0
-        for ep in range(epochs):
-            perm = torch.randperm(n_train, device=self.device, generator=g)
-            ep_loss = 0.0
-            for b in range(steps_per_epoch):
-                idx = perm[b * batch:(b + 1) * batch]
-                rate = lr * 0.5 * (1.0 + math.cos(math.pi * it / total))
-                loss, gW, gb = self.loss_and_grads(u[idx].contiguous(), y[idx].contiguous())
-                self.adam(gW, gb, rate)
-                ep_loss += loss
-                it += 1
-            val = self.relative_error(sv, envv * self.carrier(sv))
-            hist.append({"epoch": ep, "train_mse": ep_loss / steps_per_epoch, "val_rel_l2": val})
-            if log:
-                log(hist[-1])
-        torch.cuda.synchronize(self.device)
-        return {"history": hist, "train_s": time.perf_counter() - t1, "data_s": t_data, "steps": it,
-                "samples": n_train, "scale": self.scale}
+        return int(self.status.item())
 
     @torch.no_grad()
-    def predict(self, samples: torch.Tensor, chunk: int = 1 << 20, backend: str = "tc") -> torch.Tensor:
-        """Complex transmit pressure at samples (n, 4) [x, z, f, theta].  ``backend="tc"`` runs
-        the fused tensor-core forward pass, ``"simt"`` the training kernels' forward pass."""
-        out = torch.empty(samples.shape[0], dtype=torch.complex64, device=self.device)
-        for i in range(0, samples.shape[0], chunk):
-            s = samples[i:i + chunk]
-            u = self.normalise(s)
-            o = self.forward_tc(u) if backend == "tc" else self.forward(u)[0]
-            out[i:i + chunk] = torch.view_as_complex(o.contiguous()) * self.scale * self.carrier(s)
+    def predict(self, samples: torch.Tensor, chunk: int = 1 << 21) -> torch.Tensor:
+        """Complex transmit pressure at samples (n, 4) [x, z, f, theta] from the network."""
+        s = samples.to(device=self.device, dtype=torch.float64).contiguous()
+        out = torch.empty(s.shape[0], dtype=torch.complex64, device=self.device)
+        for i in range(0, s.shape[0], chunk):
+            si = s[i:i + chunk]
+            u, _ = self.inputs(si, with_aux=False)
+            net = self.forward_tc(u)
+            _check(self.lib.fsg_surrogate_combine(self.domain, si.data_ptr(), si.shape[0], net.data_ptr(), self.scale,
+                                                  out[i:i + chunk].data_ptr(), self._stream()))
         return out
 
     def relative_error(self, samples: torch.Tensor, exact: torch.Tensor) -> float:
@@ -290,11 +346,16 @@ class TxFieldSurrogate:
 
 def simus_with_surrogate(sur: TxFieldSurrogate, scat: np.ndarray, rc: np.ndarray, angles_rad, plan, *,
                          tol: float = 1e-3, tile: int = 64, judges_per_tile: int = 4, exact_reference=True) -> dict:
-    """Simus of one phantom for every firing with the transmit field from the network, each
-    scatterer tile judged by the exact kernel on `judges_per_tile` of its scatterers and
-    recomputed exactly where the relative L2 error exceeds `tol`.  Returns RF, timings and the
-    fallback fraction, plus the exact batched sweep's RF and time for comparison."""
+    """Simus of one phantom for every firing with the transmit field from the network where the
+    query lies in its domain, and from the exact kernel elsewhere.  Every (tile of scatterers,
+    firing) that used the network is judged by the exact kernel on `judges_per_tile` of its
+    scatterers over all frequencies and recomputed exactly where the relative L2 error exceeds
+    `tol`.  The receive contraction with that transmit field is the batched receive kernel.
+    Returns RF, timings, the fraction of (tile, firing) units that fell back, the share of
+    transmit-field queries the network answered, and (exact_reference) the exact batched sweep's
+    RF and time for comparison."""
     from fastsimus_gb300.batched import BatchedSimus, BatchTuning
+    from fastsimus_gb300.plan import element_positions
     from fastsimus_gb300.tx_delay import plane_wave
 
     dev = sur.device
@@ -305,65 +366,108 @@ def simus_with_surrogate(sur: TxFieldSurrogate, scat: np.ndarray, rc: np.ndarray
     f = torch.as_tensor(plan.selected_freqs, dtype=torch.float64, device=dev)
     th = torch.as_tensor(np.asarray(angles_rad, dtype=np.float64), device=dev)
     sc = torch.as_tensor(scat, dtype=torch.float64, device=dev)
-    epos, _, apex = element_positions(p.n_elements, p.pitch, p.radius)
+    epos, _, _ = element_positions(p.n_elements, p.pitch, p.radius)
     delays = np.stack([plane_wave(epos, float(a), speed_of_sound=m.speed_of_sound) for a in angles_rad])
+    n_tiles = (S + tile - 1) // tile
+    b = sur.box
+    f_in = (f >= b.f[0]) & (f <= b.f[1])
+    t_in = th.abs() <= b.max_angle
+    pt_in = (sc[:, 0] >= b.x[0]) & (sc[:, 0] <= b.x[1]) & (sc[:, 1] >= b.z[0]) & (sc[:, 1] <= b.z[1])
+    pad = torch.ones(n_tiles * tile, dtype=torch.bool, device=dev)
+    pad[:S] = pt_in
+    tile_in = pad.view(n_tiles, tile).all(dim=1)
+    use_net = tile_in[:, None] & t_in[None, :]  # (tile, firing) units the network may answer
 
-    def queries(rows: torch.Tensor) -> torch.Tensor:  # (len(rows) * F * T, 4) in [s][f][t] order
-        n = rows.shape[0]
-        q = torch.empty(n, F, T, 4, dtype=torch.float64, device=dev)
+    def queries(rows: torch.Tensor, fsel: torch.Tensor, tsel: torch.Tensor) -> torch.Tensor:
+        q = torch.empty(rows.shape[0], fsel.shape[0], tsel.shape[0], 4, dtype=torch.float64, device=dev)
         q[..., 0] = sc[rows, 0][:, None, None]
         q[..., 1] = sc[rows, 1][:, None, None]
-        q[..., 2] = f[None, :, None]
-        q[..., 3] = th[None, None, :]
+        q[..., 2] = fsel[None, :, None]
+        q[..., 3] = tsel[None, None, :]
         return q.reshape(-1, 4)
 
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
-    tx = torch.empty(S * F * T, dtype=torch.complex64, device=dev)
-    step = max(1, (1 << 22) // (F * T))
-    for i in range(0, S, step):
-        rows = torch.arange(i, min(S, i + step), device=dev)
-        tx[i * F * T:(i + rows.shape[0]) * F * T] = sur.predict(queries(rows))
+    tx = torch.empty(S, F, T, dtype=torch.complex64, device=dev)
+    # network: in-domain tiles x in-band frequencies x in-range firings; everything else exact
+    net_rows = torch.nonzero(tile_in.repeat_interleave(tile)[:S]).flatten()
+    fi, ti_ = torch.nonzero(f_in).flatten(), torch.nonzero(t_in).flatten()
+    n_net = int(net_rows.numel() * fi.numel() * ti_.numel())
+    step = max(1, (1 << 22) // max(1, fi.numel() * ti_.numel()))
+    for i in range(0, net_rows.numel(), step):
+        rows = net_rows[i:i + step]
+        val = sur.predict(queries(rows, f[fi], th[ti_])).view(rows.shape[0], fi.numel(), ti_.numel())
+        tx[rows[:, None, None], fi[None, :, None], ti_[None, None, :]] = val
     torch.cuda.synchronize(dev)
     t_net = time.perf_counter() - t0
-    # judge every tile on a few members; recompute failing tiles exactly
     t0 = time.perf_counter()
-    n_tiles = (S + tile - 1) // tile
-    failed = []
-    errs = []
-    txv = tx.view(S, F, T)
-    for ti in range(n_tiles):
-        lo, hi = ti * tile, min(S, (ti + 1) * tile)
-        judges = torch.linspace(lo, hi - 1, min(judges_per_tile, hi - lo), device=dev).round().long()
-        ex = sur.exact(queries(judges)).view(-1, F, T)
-        err = float(torch.linalg.vector_norm(txv[judges] - ex) / torch.linalg.vector_norm(ex))
-        errs.append(err)
-        if err > tol:
-            failed.append(ti)
-            rows = torch.arange(lo, hi, device=dev)
-            txv[lo:hi] = sur.exact(queries(rows)).view(-1, F, T)
+    # exact: every query the network does not answer
+    mask = torch.zeros(S, F, T, dtype=torch.bool, device=dev)
+    mask[net_rows[:, None, None], fi[None, :, None], ti_[None, None, :]] = True
+    ex_idx = torch.nonzero(~mask.view(-1)).flatten()
+    for i in range(0, ex_idx.numel(), 1 << 22):
+        idx = ex_idx[i:i + (1 << 22)]
+        s_i, rem = idx // (F * T), idx % (F * T)
+        q = torch.stack([sc[s_i, 0], sc[s_i, 1], f[rem // T], th[rem % T]], -1)
+        tx.view(-1)[idx] = sur.exact(q)
+    torch.cuda.synchronize(dev)
+    t_exact_part = time.perf_counter() - t0
+    # judge every network-answered (tile, firing) on a few members; recompute failing units exactly
+    t0 = time.perf_counter()
+    units = torch.nonzero(use_net)
+    errs = torch.zeros(0, device=dev)
+    failed_units = units[:0]
+    if units.numel():
+        n_u = units.shape[0]
+        lo = units[:, 0] * tile
+        last = torch.clamp(lo + tile, max=S) - 1
+        frac = torch.linspace(0.0, 1.0, judges_per_tile, dtype=torch.float64, device=dev)
+        jrows = (lo[:, None] + ((last - lo)[:, None].double() * frac[None, :]).round().long())  # (units, judges)
+        q = torch.empty(n_u, judges_per_tile, F, 4, dtype=torch.float64, device=dev)
+        q[..., 0] = sc[jrows, 0][..., None]
+        q[..., 1] = sc[jrows, 1][..., None]
+        q[..., 2] = f[None, None, :]
+        q[..., 3] = th[units[:, 1]][:, None, None]
+        ex = sur.exact(q.view(-1, 4)).view(n_u, judges_per_tile, F)
+        got = tx[jrows, :, units[:, 1][:, None]]  # (units, judges, F)
+        errs = torch.linalg.vector_norm((got - ex).reshape(n_u, -1), dim=1) / \
+            torch.linalg.vector_norm(ex.reshape(n_u, -1), dim=1)
+        failed_units = units[errs > tol]
+    n_fail_queries = 0
+    for ti, tf in failed_units.tolist():
+        lo_, hi_ = ti * tile, min(S, (ti + 1) * tile)
+        rows = torch.arange(lo_, hi_, device=dev)
+        tx[lo_:hi_, :, tf] = sur.exact(queries(rows, f, th[tf:tf + 1])).view(-1, F)
+        n_fail_queries += (hi_ - lo_) * int(fi.numel())
+    failed = int(failed_units.shape[0])
+    errs = errs.cpu().numpy()
     torch.cuda.synchronize(dev)
     t_judge = time.perf_counter() - t0
-    # receive contraction with the (network or exact) transmit field
-    b = BatchedSimus([(scat, rc)], delays, p, m, plans=[plan], backend="fp32", tuning=BatchTuning(2, 32768, 1))
-    lib = sur.lib
+    # receive contraction with that transmit field
+    bs = BatchedSimus([(scat, rc)], delays, p, m, plans=[plan], backend="fp32", tuning=BatchTuning(2, 32768, 1))
     t0 = time.perf_counter()
-    _check(lib.fsg_simus_batched_rx(b.probe, b.med, b._ph, b.delays.data_ptr(), T, tx.data_ptr(),
-                                    b.tuning.to_c(), b.ws.data_ptr(), b.ws.numel(), _device.stream_handle(dev)))
-    b._finish()
+    _check(sur.lib.fsg_simus_batched_rx(bs.probe, bs.med, bs._ph, bs.delays.data_ptr(), T, tx.data_ptr(),
+                                        bs.tuning.to_c(), bs.ws.data_ptr(), bs.ws.numel(), _device.stream_handle(dev)))
+    bs._finish()
     torch.cuda.synchronize(dev)
     t_rx = time.perf_counter() - t0
-    res = {"rf": b.rfs[0].clone(), "t_network_s": t_net, "t_judge_fallback_s": t_judge, "t_rx_s": t_rx,
-           "t_surrogate_total_s": t_net + t_judge + t_rx, "tiles": n_tiles, "tiles_fallback": len(failed),
-           "fallback_fraction": len(failed) / max(1, n_tiles), "tile_rel_err_median": float(np.median(errs)),
-           "queries": S * F * T}
+    n_units = n_tiles * T
+    fallback_units = n_units - int(use_net.sum()) + failed
+    res = {"rf": bs.rfs[0].clone(), "t_network_s": t_net, "t_exact_outside_domain_s": t_exact_part,
+           "t_judge_fallback_s": t_judge, "t_rx_s": t_rx,
+           "t_surrogate_total_s": t_net + t_exact_part + t_judge + t_rx, "units": n_units,
+           "units_in_domain": int(use_net.sum()), "units_failed_judge": failed,
+           "fallback_fraction": fallback_units / max(1, n_units),
+           "network_query_share": (n_net - n_fail_queries) / max(1, S * F * T),
+           "unit_rel_err_median": float(np.median(errs)) if errs.size else None,
+           "unit_rel_err_max": float(np.max(errs)) if errs.size else None, "queries": S * F * T}
     if exact_reference:
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        b.run()
+        bs.run()
         torch.cuda.synchronize(dev)
         res["t_exact_s"] = time.perf_counter() - t0
-        res["rf_exact"] = b.rfs[0].clone()
+        res["rf_exact"] = bs.rfs[0].clone()
         d = (res["rf"] - res["rf_exact"]).double()
         res["rf_rel_l2_vs_exact"] = float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(res["rf_exact"].double()))
         res["gain"] = res["t_exact_s"] / res["t_surrogate_total_s"]
@@ -371,7 +475,10 @@ def simus_with_surrogate(sur: TxFieldSurrogate, scat: np.ndarray, rc: np.ndarray
 
 
 def cfg5_box(params: TransducerParams) -> Box:
+    """The whole training domain of the learned-surrogate configuration: the imaging box
+    x in [-10, 10] mm, z in [5, 30] mm, the band fc (1 +- B / 2), steering up to 16 degrees."""
     fc, bw = params.freq_center, params.bandwidth
     return Box(x=(-10e-3, 10e-3), z=(5e-3, 30e-3), f=(fc * (1 - bw / 2), fc * (1 + bw / 2)),
                max_angle=16.0 * math.pi / 180.0)
+
 

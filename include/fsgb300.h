@@ -24,7 +24,7 @@
 extern "C" {
 #endif
 
-#define FSG_ABI_VERSION 1
+#define FSG_ABI_VERSION 2
 
 typedef enum FsgStatus {
   FSG_OK = 0,
@@ -228,21 +228,89 @@ int32_t fsg_txfield(const FsgProbe* probe, const FsgMedium* medium, double tx_n_
                     const double* samples, int64_t n, void* out, void* workspace, size_t workspace_bytes,
                     void* stream);
 
-/* MLP building blocks of the transmit-field surrogate (no counterpart in the reference).
- * fsg_mlp_gemm: C[m][n] = sum_k A(m,k) B(k,n) with A(m,k) = A[m*a_sm + k*a_sk] (float32),
- * B(k,n) = B[k*b_sk + n*b_sn] (bfloat16 if b_bf16 else float32), FP32 accumulation, and a
- * fused epilogue: 0 = (+bias[n]) (accumulate into C if `accumulate`), 1 = C = acc + bias[n],
- * C2 = silu(C), 2 = C = acc * silu'(Zs[m][n]).  C, C2, Zs have row stride ldc. */
-int32_t fsg_mlp_gemm(const float* A, int64_t a_sm, int64_t a_sk, const void* B, int64_t b_sk, int64_t b_sn,
-                     int32_t b_bf16, const float* bias, const float* Zs, float* C, float* C2, int64_t ldc, int32_t M,
-                     int32_t N, int32_t K, int32_t epilogue, int32_t accumulate, void* stream);
-/* feat[n][j] = sin(2 pi B_j . u_n), feat[n][64+j] = cos(2 pi B_j . u_n), B: [64][4], u: [n][4]. */
-int32_t fsg_mlp_features(const float* u, const float* bmat, float* feat, int64_t n, void* stream);
-/* out[n] (+)= sum_m X[m][n], X: [M][N] float32. */
-int32_t fsg_mlp_colsum(const float* X, int64_t M, int32_t N, float* out, int32_t accumulate, void* stream);
-/* One Adam step on float32 master weights w (and their bfloat16 copy w_bf16, if non-NULL). */
-int32_t fsg_mlp_adam(float* w, void* w_bf16, const float* grad, float* m1, float* m2, int64_t n, float lr, float b1,
-                     float b2, float eps, int32_t step, float grad_scale, void* stream);
+/* Analytic carriers of the transmit-field surrogate (no counterpart in the reference).  For a
+ * plane wave of angle theta on a linear array of n_elements at pitch, with k = 2 pi f / c:
+ *   c_0 = exp(i k (x sin theta + z cos theta - xmin))          (the plane wave)
+ *   c_1 = exp(i k (r_L + x_L sin theta - xmin)),  x_L = x_0 - pitch / 2
+ *   c_2 = exp(i k (r_R + x_R sin theta - xmin)),  x_R = x_{E-1} + pitch / 2
+ * (the waves of the two aperture edges; r = distance from (x, z) to the edge,
+ * xmin = min(x_0 sin theta, x_{E-1} sin theta), x_e = (e - (E-1)/2) pitch), and
+ *   c_3, c_4 = exp(i k (x sin theta_m + z cos theta_m - xmin)),  sin theta_m = sin theta + m c / (f pitch)
+ * for m = -1, +1 (the grating lobes of the pitch; zero where |sin theta_m| >= 1), phases in FP64.
+ * The box normalises u = (2 v - (lo + hi)) / (hi - lo) per input, theta by max_angle. */
+typedef struct FsgSurrogateDomain {
+  double x_lo, x_hi, z_lo, z_hi, f_lo, f_hi, max_angle;
+  double pitch, speed_of_sound;
+  int32_t n_elements;
+  int32_t n_carriers;             /* 1..5, in the order above */
+} FsgSurrogateDomain;
+
+/* samples: device [n][4] float64 (x, z, f, theta).  Writes u: [n][4] float32 (normalised) and,
+ * if aux != NULL, aux: [n][12] float32 = c_0 .. c_4 (complex; zero beyond n_carriers),
+ * field * inv_scale (complex),
+ * with field: device complex64 [n] (the exact transmit field, or NULL for zeros). */
+int32_t fsg_surrogate_inputs(const FsgSurrogateDomain* dom, const double* samples, int64_t n, const void* field,
+                             double inv_scale, float* u, float* aux, void* stream);
+/* out[i] = scale * sum_j (net[i][2j] + i net[i][2j+1]) c_j(samples[i]), complex64 [n];
+ * net: [n][2 n_carriers] float32 (the network's outputs). */
+int32_t fsg_surrogate_combine(const FsgSurrogateDomain* dom, const double* samples, int64_t n, const float* net,
+                              double scale, void* out, void* stream);
+
+/*
+ * Tensor-core training of the surrogate network (no counterpart in the reference): features
+ * [sin(2 pi B u), cos(2 pi B u)] (B: 64 x 4), hidden layers 128 -> 256 -> 256 -> 256 -> 256
+ * with SiLU, head 256 -> n_out (2 per carrier); loss mean_batch |sum_j (o_2j + i o_2j+1) c_j -
+ * y|^2 on rows drawn from the training set by a hash of (seed, step, row).  One step is three
+ * kernel launches (forward + backward on tcgen05, weight gradients on tcgen05, reduction +
+ * Adam); the step counter, the learning-rate schedule (linear warm-up, cosine decay to lr_min)
+ * and the loss history live on the device, so a sequence of steps needs no host
+ * synchronisation and can be captured in a CUDA graph.  All pointers are device memory owned
+ * by the caller.  packed_fwd[l]: fsg_mlp_tc_packed_bytes(K) bytes (the layout of
+ * fsg_mlp_tc_pack); packed_bwd[1..3]: 128 KB each.  fsg_mlp_train_init writes both packed
+ * copies from the FP32 weights and clears the workspace counters.
+ */
+typedef struct FsgMlpTrain {
+  const float* u;                 /* [n_data][4] */
+  const float* aux;               /* [n_data][12] (fsg_surrogate_inputs) */
+  int64_t n_data;
+  uint64_t seed;
+  const float* bmat;              /* [64][4] */
+  float* w[4];                    /* [256][128] (layer 0), [256][256] */
+  float* m_w[4];
+  float* v_w[4];
+  void* packed_fwd[4];
+  void* packed_bwd[4];            /* [0] unused */
+  float* b[4];                    /* [256] */
+  float* m_b[4];
+  float* v_b[4];
+  float* w_head;                  /* [n_out][256] */
+  float* m_w_head;
+  float* v_w_head;
+  float* b_head;                  /* [n_out] */
+  float* m_b_head;
+  float* v_b_head;
+  int32_t n_out;                  /* 2 n_carriers, <= 10 */
+  int32_t n_tiles;                /* batch = 128 n_tiles rows */
+  int32_t n_split;                /* row splits of the weight-gradient kernel */
+  int32_t total_steps;
+  int32_t warmup_steps;
+  float lr, lr_min, beta1, beta2, eps;
+  int32_t* step;                  /* device step counter */
+  float* loss_hist;               /* device [loss_hist_len]: mean loss of step t at [t] */
+  int32_t loss_hist_len;
+  int32_t* status;                /* device int: FSG_ETIMEOUT if a bounded wait gave up */
+  void* workspace;
+  size_t workspace_bytes;
+} FsgMlpTrain;
+
+size_t fsg_mlp_train_workspace_size(int32_t n_tiles, int32_t n_split);
+int64_t fsg_mlp_train_n_params(int32_t n_out);
+int32_t fsg_mlp_train_init(const FsgMlpTrain* t, void* stream);
+int32_t fsg_mlp_train_steps(const FsgMlpTrain* t, int32_t n_steps, void* stream);
+/* One step's gradients without the update: grads_out [fsg_mlp_train_n_params] in the order
+ * W_0, W_1, W_2, W_3 (row-major), b_0..b_3, W_head, b_head; rows_out [128 n_tiles]: the
+ * sampled rows of the training set. */
+int32_t fsg_mlp_train_gradients(const FsgMlpTrain* t, float* grads_out, int32_t* rows_out, void* stream);
 
 /*
  * fsg_simus without a workspace argument, for callers that cannot allocate device memory
@@ -268,10 +336,10 @@ size_t fsg_simus_noalloc_scratch_bytes(void);
  * Tensor-core inference of the transmit-field surrogate network (no counterpart in the
  * reference).  Network: features [sin(2 pi B u), cos(2 pi B u)] (B: 64 x 4, row-major) of the
  * normalised inputs u (n x 4), hidden layers 128 -> 256 -> 256 -> 256 -> 256 with SiLU, head
- * 256 -> 2.  packed[l]: hidden layer l's [256][K] BF16 weights rearranged by fsg_mlp_tc_pack
- * (fsg_mlp_tc_packed_bytes(K) bytes); bias[l]: 256 floats; w_head: [2][256] floats; b_head: 2.
- * out: n x 2 floats.  status: device int set to FSG_ETIMEOUT if a bounded wait gave up (the
- * caller zeroes it).
+ * 256 -> n_out (<= 10).  packed[l]: hidden layer l's [256][K] BF16 weights rearranged by
+ * fsg_mlp_tc_pack (fsg_mlp_tc_packed_bytes(K) bytes); bias[l]: 256 floats; w_head:
+ * [n_out][256] floats; b_head: n_out.  out: n x n_out floats.  status: device int set to
+ * FSG_ETIMEOUT if a bounded wait gave up (the caller zeroes it).
  */
 typedef struct FsgMlpWeights {
   const void* packed[4];
@@ -279,6 +347,8 @@ typedef struct FsgMlpWeights {
   const float* w_head;
   const float* b_head;
   const float* bmat;
+  int32_t n_out;
+  int32_t reserved0;
 } FsgMlpWeights;
 
 size_t fsg_mlp_tc_packed_bytes(int32_t n_in);

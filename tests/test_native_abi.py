@@ -48,7 +48,38 @@ def test_struct_layouts_match_header():
     assert _native.FsgProbe.baffle_impedance.offset == 48
     assert ctypes.sizeof(_native.FsgMedium) == 16
     assert ctypes.sizeof(_native.FsgFreqPlan) == 64
-    assert ctypes.sizeof(_native.FsgMlpWeights) == 11 * 8
+    assert ctypes.sizeof(_native.FsgMlpWeights) == 12 * 8
     assert _native.FsgFreqPlan.pulse_spectrum.offset == 48
     assert ctypes.sizeof(_native.FsgDasParams) == 48
     assert _native.FsgDasParams.method.offset == 40
+
+
+def test_struct_layouts_match_a_c_compiler(tmp_path):
+    """Every struct the ctypes binding declares has the size and field offsets that a C
+    compiler gives the declaration in include/fsgb300.h."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = [getattr(_native, n) for n in dir(_native)
+               if n.startswith("Fsg") and isinstance(getattr(_native, n), type)
+               and issubclass(getattr(_native, n), ctypes.Structure)]
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "fsgb300.h"', "int main(void) {"]
+    for st in structs:
+        lines.append(f'  printf("{st.__name__} %zu\\n", sizeof({st.__name__}));')
+        for f in st._fields_:
+            lines.append(f'  printf("{st.__name__}.{f[0]} %zu\\n", offsetof({st.__name__}, {f[0]}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    root = Path(__file__).resolve().parent.parent
+    subprocess.run([cc, "-I", str(root / "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                       check=True).stdout.splitlines())
+    for st in structs:
+        assert int(got[st.__name__]) == ctypes.sizeof(st), st.__name__
+        for f in st._fields_:
+            assert int(got[f"{st.__name__}.{f[0]}"]) == getattr(st, f[0]).offset, f"{st.__name__}.{f[0]}"

@@ -1,6 +1,7 @@
-"""Transmit-field surrogate: the exact field kernel against the FP64 oracle, the network's
-hand-written forward/backward kernels against an FP64 gradient oracle, training, and the
-simus experiment with exact fallback (which reports the measured gain, positive or not)."""
+"""Transmit-field surrogate: the exact field kernel and the carriers against the FP64 oracle, the
+tensor-core training kernels' gradients and the tensor-core inference against an FP64 network
+oracle, training to the 1e-3 tolerance over the whole training box, and the simus use with exact
+fallback, which records what the trained network gains (or loses) against the exact path."""
 
 import math
 
@@ -13,6 +14,9 @@ from tests import _golden as G
 from tests._gpu import np64, require_gpu, torch
 
 pytestmark = pytest.mark.gpu
+
+SURROGATE_TOL = 1e-3       # relative L2 of the transmit field, the surrogate path's target
+BF16_GRAD_TOL = 1e-2       # weight gradients: the gradient GEMMs take BF16 operands (2^-9 rounding)
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -57,73 +61,125 @@ def test_txfield_equals_pfield_pressure_on_plan_grid():
     assert G.rel_l2(got, ref[:, k]) < 1e-5
 
 
-def test_network_gradients_match_fp64_oracle():
+def test_inputs_and_carriers_match_oracle():
+    sur = _surrogate()
+    s = sur.sample_domain(2000, seed=4)
+    field = sur.exact(s)
+    sur.scale = 2.5
+    u, aux = sur.inputs(s, field)
+    sn = s.cpu().numpy()
+    c = M.carriers(sn, sur.params.n_elements, sur.params.pitch, sur.medium.speed_of_sound)
+    a = aux.double().cpu().numpy()
+    got_c = a[:, 0:10:2] + 1j * a[:, 1:10:2]
+    assert np.max(np.abs(got_c - c)) < 1e-6
+    assert (np.abs(c[:, 3:]) == 0).any() and (np.abs(c[:, 3:]) > 0).any()  # grating lobes on and off
+    assert G.rel_l2(M.target(a), np64(field) / 2.5) < 1e-6
+    b = sur.box
+    lo = np.array([b.x[0], b.z[0], b.f[0], -b.max_angle])
+    hi = np.array([b.x[1], b.z[1], b.f[1], b.max_angle])
+    ref_u = (2 * sn - (lo + hi)) / (hi - lo)
+    ref_u[:, 3] = sn[:, 3] / b.max_angle
+    assert np.max(np.abs(u.double().cpu().numpy() - ref_u)) < 1e-6
+
+
+def test_training_gradients_match_fp64_oracle():
+    """One step of the tensor-core training kernels (forward with hi + lo BF16 activations,
+    backward and weight gradients on BF16 operands, FP32 accumulation) against the FP64
+    restatement on the same sampled rows and the same (BF16-rounded) weights."""
     sur = _surrogate(seed=4)
-    n = 96
-    s = sur.sample_domain(n, seed=5)
-    u = sur.normalise(s)
-    y = torch.randn(n, 2, device=sur.device, generator=torch.Generator(device=sur.device).manual_seed(1))
-    loss, gW, gb = sur.loss_and_grads(u, y)
-    Wd = [w.to(torch.bfloat16).double().cpu().numpy() for w in sur.W]  # kernels read BF16 weights
-    bd = [b.double().cpu().numpy() for b in sur.b]
-    l2, rW, rb = M.loss_and_grads(u.double().cpu().numpy(), y.double().cpu().numpy(),
-                                  sur.bmat.double().cpu().numpy(), Wd, bd)
-    assert abs(loss - l2) / l2 < 1e-4
-    for a, r in zip(gW + gb, rW + rb):
-        assert G.rel_l2(a.double().cpu().numpy(), r) < 1e-4
+    s, u, aux, _ = sur.make_dataset(4096, seed=5)
+    gW, gb, rows = sur.gradients(u, aux, n_tiles=2, n_split=3, seed=11)
+    r = rows.cpu().numpy()
+    assert r.min() >= 0 and r.max() < 4096 and len(np.unique(r)) > 200
+    bmat, Wd, bd = sur.oracle_params()
+    _, rW, rb = M.carrier_loss_and_grads(u.double().cpu().numpy()[r], aux.double().cpu().numpy()[r], bmat, Wd, bd)
+    for i, (a, ref) in enumerate(zip(gW, rW)):
+        e = G.rel_l2(a.double().cpu().numpy(), ref)
+        print(f"dW[{i}] relL2 {e:.2e}")
+        assert e < BF16_GRAD_TOL
+    for i, (a, ref) in enumerate(zip(gb, rb)):
+        e = G.rel_l2(a.double().cpu().numpy(), ref)
+        print(f"db[{i}] relL2 {e:.2e}")
+        assert e < (1e-4 if i == len(gb) - 1 else BF16_GRAD_TOL)  # the head bias sums FP32 outputs
 
 
-def test_tc_forward_matches_training_forward():
+def test_tc_forward_matches_fp64_oracle():
     """The fused tcgen05 inference kernel (BF16 weights, hi + lo BF16 activations, FP32
-    accumulation in TMEM) against the training kernels' FP32-activation forward pass."""
+    accumulation in TMEM) against the FP64 network with the same weights."""
     sur = _surrogate(seed=6)
+    bmat, Wd, bd = sur.oracle_params()
     for n in (1000, 128, 1):  # ragged last tile, exactly one tile, a single query
         s = sur.sample_domain(n, seed=9 + n)
-        u = sur.normalise(s)
-        ref, _ = sur.forward(u)
+        u, _ = sur.inputs(s, with_aux=False)
         got = sur.forward_tc(u)
         torch.cuda.synchronize()
         assert sur.tc_status() == 0
-        err = G.rel_l2(got.double().cpu().numpy(), ref.double().cpu().numpy())
-        print(f"tc forward n={n}: relL2 vs training forward {err:.2e}")
+        ref, _, _ = M.forward(u.double().cpu().numpy(), bmat, Wd, bd)
+        err = G.rel_l2(got.double().cpu().numpy(), ref)
+        print(f"tc forward n={n}: relL2 vs FP64 {err:.2e}")
         assert err < 1e-4
-    # after an optimiser step the packed weights follow the new values
-    y = torch.zeros(256, 2, device=sur.device)
-    u = sur.normalise(sur.sample_domain(256, seed=3))
-    _, gW, gb = sur.loss_and_grads(u, y)
-    sur.adam(gW, gb, 1e-2)
-    ref, _ = sur.forward(u)
-    got = sur.forward_tc(u)
-    assert G.rel_l2(got.double().cpu().numpy(), ref.double().cpu().numpy()) < 1e-4
 
 
-def test_training_reduces_error():
+@pytest.fixture(scope="module")
+def trained():
     sur = _surrogate(seed=1)
-    rep = sur.train(n_train=40960, epochs=4, batch=2048, lr=3e-3, n_val=4096)
-    h = rep["history"]
-    assert h[-1]["train_mse"] < h[0]["train_mse"]
-    assert h[-1]["val_rel_l2"] < 1.0
+    rep = sur.train(n_train=2_000_000, steps=60_000, lr=3e-3, evals=3,
+                    log=lambda r: print(f"step {r['step']}: loss {r['train_loss']:.3e} val {r['val_rel_l2']:.3e}"))
+    return sur, rep
 
 
-def test_simus_with_surrogate_fallback_is_exact():
-    """With the 1e-3 tolerance every tile the network cannot meet is recomputed by the exact
-    kernel; the RF then matches the exact batched sweep at FP32 level.  The timing fields are
-    the honest gain measurement."""
+def test_training_meets_the_tolerance_over_the_box(trained):
+    sur, rep = trained
+    print({k: v for k, v in rep.items() if k not in ("history", "loss_curve")})
+    peaks = {}
+    try:
+        import json
+        from pathlib import Path
+
+        peaks = json.loads((Path(__file__).resolve().parent.parent / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    if "bf16_tflops" in peaks:
+        print(f"training: {rep['algorithmic_tflops']:.1f} TFLOP/s = {rep['algorithmic_tflops'] / peaks['bf16_tflops']:.3f}"
+              " of the measured BF16 peak")
+    assert rep["history"][-1]["train_loss"] < rep["history"][0]["train_loss"]
+    # an independent check on fresh samples of the box
+    s = sur.sample_domain(262_144, seed=77)
+    err = sur.relative_error(s, sur.exact(s))
+    print(f"val relL2 {rep['val_rel_l2']:.3e}, fresh-sample relL2 {err:.3e}")
+    assert rep["val_rel_l2"] <= SURROGATE_TOL
+    assert err <= SURROGATE_TOL
+
+
+def test_simus_with_the_trained_surrogate_records_its_gain(trained):
+    """A phantom inside the training box, firings inside its angle range: the network answers
+    the queries inside its band, the judge accepts (tile, firing) units at 1e-3, and the RF
+    agrees with the exact batched sweep; the timings record the gain against the exact path
+    (below 1 here: the batched sweep shares each Green's term between the firings, which a
+    per-query network cannot)."""
     from fastsimus_gb300 import workloads as W
     from fastsimus_gb300.batched import shared_plan
     from fastsimus_gb300.surrogate import simus_with_surrogate
 
-    p, m = W.cfg1_probe(), W.cfg1_medium()
-    sur = _surrogate(seed=2)
-    sur.train(n_train=20480, epochs=2, batch=2048, n_val=2048)
-    s, r = W.cfg1_scatterers(192, seed=8)
-    angles = np.deg2rad([-10.0, 0.0, 10.0])
+    sur, _ = trained
+    p, m = sur.params, sur.medium
+    b = sur.box
+    rng = np.random.default_rng(8)
+    s = W._f32(np.stack([rng.uniform(b.x[0], b.x[1], 512), rng.uniform(b.z[0], b.z[1], 512)], -1))
+    r = rng.standard_normal(512)
+    angles = np.deg2rad([-15.0, -6.0, 0.0, 4.0, 15.5])
     delays = W.plane_wave_delays(p, m, np.rad2deg(angles))
     plan = shared_plan(s, r, list(delays), p, m)
-    res = simus_with_surrogate(sur, s, r, angles, plan, tol=1e-3)
-    print({k: v for k, v in res.items() if not k.startswith("rf")})
-    if res["fallback_fraction"] == 1.0:
-        assert res["rf_rel_l2_vs_exact"] < 1e-5
-    loose = simus_with_surrogate(sur, s, r, angles, plan, tol=math.inf)
-    assert loose["fallback_fraction"] == 0.0
-    assert np.isfinite(loose["rf_rel_l2_vs_exact"])
+    res = simus_with_surrogate(sur, s, r, angles, plan, tol=SURROGATE_TOL)
+    print({k: v for k, v in res.items() if not k.startswith("rf") or k == "rf_rel_l2_vs_exact"})
+    assert res["fallback_fraction"] < 1.0
+    assert res["network_query_share"] > 0.3
+    assert res["rf_rel_l2_vs_exact"] < SURROGATE_TOL
+    assert "gain" in res and res["gain"] > 0
+    # outside the network's domain every query is exact: the RF then equals the exact sweep
+    s_out = W._f32(np.stack([rng.uniform(-14e-3, -11e-3, 128), rng.uniform(31e-3, 35e-3, 128)], -1))
+    r_out = rng.standard_normal(128)
+    plan2 = shared_plan(s_out, r_out, list(delays), p, m)
+    res2 = simus_with_surrogate(sur, s_out, r_out, angles, plan2, tol=SURROGATE_TOL)
+    assert res2["fallback_fraction"] == 1.0 and res2["network_query_share"] == 0.0
+    assert res2["rf_rel_l2_vs_exact"] < 1e-5
