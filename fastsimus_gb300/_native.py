@@ -73,7 +73,7 @@ class FsgMlpTrain(ctypes.Structure):
                 ("b", _V4), ("m_b", _V4), ("v_b", _V4),
                 ("w_head", ctypes.c_void_p), ("m_w_head", ctypes.c_void_p), ("v_w_head", ctypes.c_void_p),
                 ("b_head", ctypes.c_void_p), ("m_b_head", ctypes.c_void_p), ("v_b_head", ctypes.c_void_p),
-                ("n_out", ctypes.c_int32), ("n_tiles", ctypes.c_int32), ("n_split", ctypes.c_int32),
+                ("packed_head", ctypes.c_void_p), ("n_out", ctypes.c_int32), ("n_tiles", ctypes.c_int32), ("n_split", ctypes.c_int32),
                 ("total_steps", ctypes.c_int32), ("warmup_steps", ctypes.c_int32),
                 ("lr", ctypes.c_float), ("lr_min", ctypes.c_float), ("beta1", ctypes.c_float),
                 ("beta2", ctypes.c_float), ("eps", ctypes.c_float),

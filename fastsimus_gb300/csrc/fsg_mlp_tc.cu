@@ -166,7 +166,8 @@ __global__ void __launch_bounds__(256, 1) mlp_tc_forward_kernel(const __grid_con
             const int kk = c * (kMlpChunkK / 16) + ks;  // K step of 16 within the layer
             const uint64_t ah = tc::sdesc(sbase + kOffAHi + kk * 256, 128, kMlpKGroups * 128);
             const uint64_t al = tc::sdesc(sbase + kOffALo + kk * 256, 128, kMlpKGroups * 128);
-            const uint64_t bd = tc::sdesc(bb + ks * 256, 128, (kMlpChunkK / 8) * 128);
+            // k-group-major packed chunk: K stride 4096 bytes, N stride 128
+            const uint64_t bd = tc::sdesc(bb + ks * 2 * 4096, 4096, 128);
             tc::mma_bf16(tmem, ah, bd, idesc, kk > 0);
             tc::mma_bf16(tmem, al, bd, idesc, 1);
           }
@@ -243,7 +244,8 @@ __global__ void mlp_pack_kernel(const __nv_bfloat16* __restrict__ w, int K, __nv
   if (i >= kMlpWidth * K) return;
   const int n = i / K, k = i % K;
   const int c = k / kMlpChunkK, kk = k % kMlpChunkK;
-  const uint32_t off = tc::kmajor_off(n, kk, kMlpChunkK / 8);  // bytes within the chunk
+  // bytes within the chunk: core (kk / 8, n / 8) at ((kk / 8) * 32 + n / 8) * 128 (k-group-major)
+  const uint32_t off = ((uint32_t)(((kk >> 3) << 5) + (n >> 3)) << 7) + ((uint32_t)(n & 7) << 4) + ((uint32_t)(kk & 7) << 1);
   packed[(size_t)c * (kMlpChunkBytes / 2) + off / 2] = w[i];
 }
 

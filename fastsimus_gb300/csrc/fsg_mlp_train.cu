@@ -48,13 +48,33 @@ constexpr int kMaxOut = 10;                           // head outputs (2 per car
 constexpr int kAux = 12;                              // per row: carriers c_0..c_4, target y (complex)
 constexpr int kHO = 16;                               // head width padded for the weight-gradient MMA
 constexpr int kPart = kHO + 1;                        // per-tile partials: head-bias gradients, loss
-constexpr int kChunkK = 64;                           // K columns per streamed weight chunk
+// Packed weights (global): chunks of 64 inputs (forward, K-major) or 64 outputs (backward,
+// MN-major), 32 KB each, core matrices k-group-major so that each half chunk of 32 K columns is
+// a contiguous 16 KB piece.  The kernels stream 16 KB pieces through kBufs buffers.
+constexpr int kChunkK = 64;                           // K columns per packed chunk
 constexpr uint32_t kChunkBytes = kW * kChunkK * 2;    // 32 KB
+constexpr int kPieceK = 64;                           // K columns per streamed piece (32 or 64)
+constexpr uint32_t kPieceBytes = kW * kPieceK * 2;    // 16 KB
+constexpr int kBufs = kPieceK == 32 ? 5 : 2;          // streamed pieces in shared memory
 constexpr uint32_t kABytes = kRows * kW * 2;          // one BF16 copy of a 128 x 256 operand
-constexpr uint32_t kOffAHi = 0, kOffALo = kABytes, kOffB0 = 2 * kABytes, kOffB1 = kOffB0 + kChunkBytes;
-constexpr uint32_t kFbSmem = kOffB1 + kChunkBytes;
-constexpr int kChunksPerTile = 2 + 3 * 4 + 3 * 4;     // forward 2 + 4 + 4 + 4, backward 4 + 4 + 4
+constexpr uint32_t kOffAHi = 0, kOffALo = kABytes, kOffB = 2 * kABytes;
+constexpr uint32_t kFbSmem = kOffB + kBufs * kPieceBytes;
+// The head's packed weights: W_h hi and lo (K-major, 16 rows x 256, row-group-major cores; the
+// forward MMA N = 16), one 16 KB piece, then W_h as the MN-major B operand of dA_4 = dOut W_h
+// (K = 16), an 8 KB piece.
+constexpr uint32_t kHeadHi = 0, kHeadLo = 8192, kHeadBwd = 16384, kHeadBytes = 24576;
+// Pieces of one tile: forward (layer 0: P0, layers 1..3: P1 each), the head's two, backward
+// (P1 per layer).
+constexpr int kP0 = kFeat / kPieceK, kP1 = kW / kPieceK;
+constexpr int kHeadPiece = kP0 + 3 * kP1;
+constexpr int kPiecesPerTile = kHeadPiece + 2 + 3 * kP1;
 constexpr uint32_t kWaitTries = 1u << 26;
+
+// Byte offset of (row n, input k) inside a 64-input packed chunk, k-group-major: core
+// (k / 8, n / 8) at ((k / 8) * 32 + n / 8) * 128.  MMA descriptor: LBO (K) 4096, SBO (N) 128.
+__host__ __device__ inline uint32_t wpack_off(int n, int k) {
+  return ((uint32_t)(((k >> 3) << 5) + (n >> 3)) << 7) + ((uint32_t)(n & 7) << 4) + ((uint32_t)(k & 7) << 1);
+}
 
 // Global stash, per 64-row chunk q of the batch.  "A-role" tensors feed the weight-gradient
 // MMA as its A operand (M = feature): two 16 KB halves of 128 features, each MN-major core
@@ -85,7 +105,7 @@ struct Net {
   const void* wf[4];       // forward-packed BF16 (K-major chunks of 64 inputs)
   const void* wb[4];       // backward-packed BF16 (MN-major chunks of 64 outputs), [1..3]
   const float* bias[4];
-  const float* whead;      // [n_out][256]
+  const void* whead;       // packed head weights (kHeadBytes)
   const float* bhead;      // [n_out]
   int n_out;
 };
@@ -140,30 +160,39 @@ __device__ __forceinline__ unsigned char* chunk_ptr(unsigned char* base, size_t 
   return base + (size_t)(tile * 2 + (R >> 6)) * chunk_bytes;
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 __global__ void __launch_bounds__(256, 1) mlp_train_fb_kernel(const __grid_constant__ FbArgs a) {
   extern __shared__ __align__(1024) unsigned char sm[];
-  __shared__ uint64_t mbar_full[2], mbar_free[2], mbar_mma;
+  __shared__ uint64_t mbar_full[kBufs], mbar_free[kBufs], mbar_mma;
   __shared__ uint32_t tmem_holder;
   __shared__ int s_fail;
   __shared__ int s_step;
   __shared__ float s_bmat[256];
   __shared__ float s_bias[4][kW];
-  __shared__ float s_wh[kMaxOut][kW];
   __shared__ float s_bh[kMaxOut];
   __shared__ float4 s_u[kRows];
   __shared__ float s_aux[kRows][kAux];
-  __shared__ float s_out[kRows][kMaxOut];
   __shared__ float s_red[4][kPart];
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nout = a.net.n_out;
   for (int i = tid; i < 256; i += blockDim.x) s_bmat[i] = a.net.bmat[i];
   for (int i = tid; i < 4 * kW; i += blockDim.x) s_bias[i / kW][i % kW] = a.net.bias[i / kW][i % kW];
-  for (int i = tid; i < kMaxOut * kW; i += blockDim.x)
-    s_wh[i / kW][i % kW] = (i / kW < nout) ? a.net.whead[i] : 0.f;
   if (tid < kMaxOut) s_bh[tid] = tid < nout ? a.net.bhead[tid] : 0.f;
   if (tid == 0) {
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < kBufs; ++b) {
       tc::mbar_init(&mbar_full[b], 1);
       tc::mbar_init(&mbar_free[b], 1);
     }
@@ -172,7 +201,9 @@ __global__ void __launch_bounds__(256, 1) mlp_train_fb_kernel(const __grid_const
     s_fail = 0;
     s_step = *a.step;
   }
-  if (warp == 0) tc::tmem_alloc(&tmem_holder, kW);
+  // TMEM: columns [0, 256) the layer accumulator; [256, 272) the head's outputs, then
+  // [256, 512) dA_4 = dOut W_h
+  if (warp == 0) tc::tmem_alloc(&tmem_holder, 2 * kW);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -180,68 +211,136 @@ __global__ void __launch_bounds__(256, 1) mlp_train_fb_kernel(const __grid_const
   const uint32_t sbase = tc::smem_u32(sm);
   const uint32_t id_fwd = tc::idesc_bf16(kRows, kW, 0, 0);  // A K-major, B K-major
   const uint32_t id_bwd = tc::idesc_bf16(kRows, kW, 0, 1);  // A K-major, B MN-major
+  const uint32_t id_head = tc::idesc_bf16(kRows, kHO, 0, 0); // head: N = 16
   const uint64_t step_key = (uint64_t)(uint32_t)s_step << 32;
 
-  // Weight chunks as one sequence over all tiles: chunk g of a tile is j = g % kChunksPerTile.
-  uint32_t ph_full[2] = {0u, 0u}, ph_free[2] = {0u, 0u}, ph_mma = 0u;
-  int64_t next_load = 0, consumed = 0;  // chunks copied / chunks whose copy was waited for
+  // Weight pieces as one sequence over all tiles: piece g of a tile is j = g % kPiecesPerTile,
+  // held in buffer g % kBufs; up to kBufs pieces are in flight.
+  uint32_t ph_full[kBufs] = {}, ph_free[kBufs] = {}, ph_mma = 0u;
+  int64_t next_load = 0, consumed = 0;  // pieces copied / pieces whose copy was waited for
   const int64_t my_tiles = (a.n_tiles - (int64_t)blockIdx.x + gridDim.x - 1) / gridDim.x;
-  const int64_t total_chunks = my_tiles * kChunksPerTile;
-  auto load = [&](int64_t g) -> bool {
-    const int b = (int)(g & 1);
-    if (g >= 2) {
-      if (!tc::mbar_wait_bounded(&mbar_free[b], ph_free[b], kWaitTries)) return false;
+  const int64_t total_pieces = my_tiles * kPiecesPerTile;
+  // Copies piece g into buffer g % kBufs.  The buffer's previous piece (g - kBufs) must be
+  // released by its MMAs: with `block` the call waits for that (bounded); without, it returns
+  // false at once (nothing issued) if the release has not happened yet.
+  auto load = [&](int64_t g, bool block, bool& failed) -> bool {
+    const int b = (int)(g % kBufs);
+    if (g >= kBufs) {
+      if (block) {
+        if (!tc::mbar_wait_bounded(&mbar_free[b], ph_free[b], kWaitTries)) {
+          failed = true;
+          return false;
+        }
+      } else if (!tc::mbar_test(&mbar_free[b], ph_free[b])) {
+        return false;
+      }
       ph_free[b] ^= 1u;
     }
-    const int j = (int)(g % kChunksPerTile);
+    const int j = (int)(g % kPiecesPerTile);
     const unsigned char* src;
-    if (j < 2) {
-      src = static_cast<const unsigned char*>(a.net.wf[0]) + (size_t)j * kChunkBytes;
-    } else if (j < 14) {
-      src = static_cast<const unsigned char*>(a.net.wf[1 + (j - 2) / 4]) + (size_t)((j - 2) % 4) * kChunkBytes;
+    uint32_t bytes = kPieceBytes;
+    if (j < kP0) {
+      src = static_cast<const unsigned char*>(a.net.wf[0]) + (size_t)j * kPieceBytes;
+    } else if (j < kHeadPiece) {
+      src = static_cast<const unsigned char*>(a.net.wf[1 + (j - kP0) / kP1]) + (size_t)((j - kP0) % kP1) * kPieceBytes;
+    } else if (j == kHeadPiece) {
+      src = static_cast<const unsigned char*>(a.net.whead) + kHeadHi;  // hi and lo, 16 KB
+    } else if (j == kHeadPiece + 1) {
+      src = static_cast<const unsigned char*>(a.net.whead) + kHeadBwd;
+      bytes = kHeadBytes - kHeadBwd;
     } else {
-      src = static_cast<const unsigned char*>(a.net.wb[3 - (j - 14) / 4]) + (size_t)((j - 14) % 4) * kChunkBytes;
+      const int q = j - kHeadPiece - 2;
+      src = static_cast<const unsigned char*>(a.net.wb[3 - q / kP1]) + (size_t)(q % kP1) * kPieceBytes;
     }
-    tc::mbar_arrive_expect_tx(&mbar_full[b], kChunkBytes);
-    tc::bulk_g2s(sm + (b ? kOffB1 : kOffB0), src, kChunkBytes, &mbar_full[b]);
+    tc::mbar_arrive_expect_tx(&mbar_full[b], bytes);
+    tc::bulk_g2s(sm + kOffB + b * kPieceBytes, src, bytes, &mbar_full[b]);
     return true;
   };
-  // One GEMM of the tile on the tensor cores (thread 0): nch chunks of 4 K-steps of 16.
+  // Wait for piece g (loading ahead up to kBufs pieces); returns its buffer's shared address.
+  // Look-ahead copies never wait for the MMAs of the pieces just issued (that would drain the
+  // tensor pipe between pieces): only the piece needed now may block.
+  auto acquire = [&](int64_t g, uint32_t& addr) -> bool {
+    bool failed = false;
+    while (next_load < g + kBufs && next_load < total_pieces) {
+      if (!load(next_load, next_load <= g, failed)) {
+        if (failed) return false;
+        break;
+      }
+      ++next_load;
+    }
+    const int b = (int)(g % kBufs);
+    if (!tc::mbar_wait_bounded(&mbar_full[b], ph_full[b], kWaitTries)) return false;
+    ph_full[b] ^= 1u;
+    ++consumed;
+    tc::fence_after_sync();
+    addr = sbase + kOffB + b * kPieceBytes;
+    return true;
+  };
+  auto finish = [&]() -> bool {  // wait for all issued MMAs
+    tc::commit(&mbar_mma);
+    if (!tc::mbar_wait_bounded(&mbar_mma, ph_mma, kWaitTries)) return false;
+    ph_mma ^= 1u;
+    return true;
+  };
+  // One GEMM of the tile on the tensor cores (thread 0): np pieces of 2 K-steps of 16.
   // Forward: D = A_hi W^T + A_lo W^T; backward: D = dZ W (dZ in the A_hi region).
-  auto gemm = [&](int64_t chunk0, int nch, bool bwd) -> bool {
-    for (int c = 0; c < nch; ++c) {
-      const int64_t g = chunk0 + c;
-      const int b = (int)(g & 1);
-      while (next_load < g + 2 && next_load < total_chunks)
-        if (!load(next_load++)) return false;
-      if (!tc::mbar_wait_bounded(&mbar_full[b], ph_full[b], kWaitTries)) return false;
-      ph_full[b] ^= 1u;
-      ++consumed;
-      tc::fence_after_sync();
-      const uint32_t bb = sbase + (b ? kOffB1 : kOffB0);
+  auto gemm = [&](int64_t piece0, int np, bool bwd) -> bool {
+    for (int c = 0; c < np; ++c) {
+      const int64_t g = piece0 + c;
+      uint32_t bb;
+      if (!acquire(g, bb)) return false;
 #pragma unroll
-      for (int ks = 0; ks < kChunkK / 16; ++ks) {
-        const int kk = c * (kChunkK / 16) + ks;
+      for (int ks = 0; ks < kPieceK / 16; ++ks) {
+        const int kk = c * (kPieceK / 16) + ks;
         const uint64_t ah = tc::sdesc(sbase + kOffAHi + kk * 256, 128, 32 * 128);
+        const uint64_t bd = tc::sdesc(bb + ks * 2 * 4096, 4096, 128);  // both packings: K stride 4096, N stride 128
         if (!bwd) {
-          const uint64_t bd = tc::sdesc(bb + ks * 256, 128, 8 * 128);
           const uint64_t al = tc::sdesc(sbase + kOffALo + kk * 256, 128, 32 * 128);
           tc::mma_bf16(tmem, ah, bd, id_fwd, kk > 0);
           tc::mma_bf16(tmem, al, bd, id_fwd, 1);
         } else {
-          const uint64_t bd = tc::sdesc(bb + ks * 2 * 4096, 4096, 128);
           tc::mma_bf16(tmem, ah, bd, id_bwd, kk > 0);
         }
       }
-      tc::commit(&mbar_free[b]);
+      tc::commit(&mbar_free[(int)(g % kBufs)]);
     }
-    tc::commit(&mbar_mma);
-    if (!tc::mbar_wait_bounded(&mbar_mma, ph_mma, kWaitTries)) return false;
-    ph_mma ^= 1u;
-    // both buffers are free now: start the next two copies so they land during the epilogue
-    while (next_load < chunk0 + nch + 2 && next_load < total_chunks)
-      if (!load(next_load++)) return false;
+    if (!finish()) return false;
+    // every buffer is free now: start the next pieces so they land during the epilogue
+    bool failed = false;
+    while (next_load < piece0 + np + kBufs && next_load < total_pieces) {
+      if (!load(next_load, true, failed)) return false;
+      ++next_load;
+    }
     return true;
+  };
+  // The head's forward MMA (thread 0): O = A_4 W_h^T in TMEM columns [256, 272), three products
+  // A_hi W_hi + A_lo W_hi + A_hi W_lo over K = 256.
+  auto head_fwd = [&](int64_t g) -> bool {
+    uint32_t hb;
+    if (!acquire(g, hb)) return false;
+#pragma unroll
+    for (int kk = 0; kk < kW / 16; ++kk) {
+      const uint64_t ah = tc::sdesc(sbase + kOffAHi + kk * 256, 128, 32 * 128);
+      const uint64_t al = tc::sdesc(sbase + kOffALo + kk * 256, 128, 32 * 128);
+      const uint64_t bh = tc::sdesc(hb + kHeadHi + kk * 256, 128, 32 * 128);
+      const uint64_t bl = tc::sdesc(hb + kHeadLo + kk * 256, 128, 32 * 128);
+      tc::mma_bf16(tmem + kW, ah, bh, id_head, kk > 0);
+      tc::mma_bf16(tmem + kW, al, bh, id_head, 1);
+      tc::mma_bf16(tmem + kW, ah, bl, id_head, 1);
+    }
+    tc::commit(&mbar_free[(int)(g % kBufs)]);
+    return finish();
+  };
+  // dA_4 = dOut W_h (K = 16; dOut as BF16 in the A_lo region, K-major [128][16]) into TMEM
+  // columns [256, 512).
+  auto head_bwd = [&](int64_t g) -> bool {
+    uint32_t hb;
+    if (!acquire(g, hb)) return false;
+    const uint64_t ad = tc::sdesc(sbase + kOffALo, 128, 2 * 128);
+    const uint64_t bd = tc::sdesc(hb, 32 * 128, 128);
+    tc::mma_bf16(tmem + kW, ad, bd, id_bwd, 0u);
+    tc::commit(&mbar_free[(int)(g % kBufs)]);
+    return finish();
   };
   auto sync_all = [&]() {
     tc::fence_before_sync();
@@ -253,7 +352,7 @@ __global__ void __launch_bounds__(256, 1) mlp_train_fb_kernel(const __grid_const
   const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
   int64_t tile_iter = 0;
   for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x, ++tile_iter) {
-    const int64_t chunk_base = tile_iter * kChunksPerTile;
+    const int64_t chunk_base = tile_iter * kPiecesPerTile;
     // ---- gather the tile's rows ----
     if (tid < kRows) {
       const uint64_t h = mix64(a.seed ^ (step_key + (uint64_t)tile * kRows + tid));
@@ -302,15 +401,12 @@ __global__ void __launch_bounds__(256, 1) mlp_train_fb_kernel(const __grid_const
     sync_all();
 
     // ---- forward ----
-    float hp[kMaxOut];
-#pragma unroll
-    for (int j = 0; j < kMaxOut; ++j) hp[j] = 0.f;
     int64_t ch = chunk_base;
     for (int l = 0; l < 4; ++l) {
-      const int nch = l == 0 ? 2 : 4;
+      const int np = l == 0 ? kP0 : kP1;
       if (tid == 0 && !s_fail)
-        if (!gemm(ch, nch, false)) s_fail = 1;
-      ch += nch;
+        if (!gemm(ch, np, false)) s_fail = 1;
+      ch += np;
       sync_all();
       if (s_fail) break;
       unsigned char* gact = chunk_ptr(a.st.act[l + 1], act_chunk_bytes(l + 1), tile, row);
@@ -332,22 +428,14 @@ __global__ void __launch_bounds__(256, 1) mlp_train_fb_kernel(const __grid_const
           const int c8 = col0 + 8 * g8;
           uint4 hi, lo;
           tc::split8(v + 8 * g8, hi, lo);
+          // the next MMA's A operand (the last layer's output feeds the head)
+          *reinterpret_cast<uint4*>(sm + kOffAHi + tc::kmajor_off(row, c8, 32)) = hi;
+          *reinterpret_cast<uint4*>(sm + kOffALo + tc::kmajor_off(row, c8, 32)) = lo;
           if (l < 3) {
-            *reinterpret_cast<uint4*>(sm + kOffAHi + tc::kmajor_off(row, c8, 32)) = hi;
-            *reinterpret_cast<uint4*>(sm + kOffALo + tc::kmajor_off(row, c8, 32)) = lo;
             *reinterpret_cast<uint4*>(gact + brole_off(row & 63, c8, kW)) = hi;
             *reinterpret_cast<uint4*>(ggate + ((size_t)(col0 >> 5) * kRows + row) * 64 + 16 * g8) = pack8(gt + 8 * g8);
           } else {
             *reinterpret_cast<uint4*>(gact + arole_off(row & 63, c8)) = hi;
-          }
-        }
-        if (l == 3) {
-#pragma unroll
-          for (int j = 0; j < kMaxOut; ++j) {
-            float acc = hp[j];
-#pragma unroll
-            for (int i = 0; i < 32; ++i) acc = fmaf(v[i], s_wh[j][col0 + i], acc);
-            hp[j] = acc;
           }
         }
       }
@@ -356,16 +444,17 @@ __global__ void __launch_bounds__(256, 1) mlp_train_fb_kernel(const __grid_const
     }
     if (s_fail) break;
 
-    // ---- head, loss and the head's output gradient ----
-    if (chalf == 1) {
-#pragma unroll
-      for (int j = 0; j < kMaxOut; ++j) s_out[row][j] = hp[j];
-    }
-    __syncthreads();
+    // ---- head on the tensor cores, loss and the head's output gradient ----
+    if (tid == 0 && !s_fail)
+      if (!head_fwd(ch)) s_fail = 1;
+    ch += 1;
+    sync_all();
+    if (s_fail) break;
     if (chalf == 0) {
-      float o[kMaxOut], d[kMaxOut];
+      float o[kHO], d[kMaxOut];
+      tmem_ld16(trow + kW, o);
 #pragma unroll
-      for (int j = 0; j < kMaxOut; ++j) o[j] = hp[j] + s_out[row][j] + s_bh[j];
+      for (int j = 0; j < kMaxOut; ++j) o[j] += s_bh[j];
       float pr = 0.f, pi = 0.f;
 #pragma unroll
       for (int c = 0; c < kMaxOut / 2; ++c) {
@@ -388,11 +477,13 @@ __global__ void __launch_bounds__(256, 1) mlp_train_fb_kernel(const __grid_const
       float d16[16];
 #pragma unroll
       for (int j = 0; j < 16; ++j) d16[j] = j < kMaxOut ? d[j] : 0.f;
+      const uint4 p0 = pack8(d16), p1 = pack8(d16 + 8);
       unsigned char* gd = chunk_ptr(a.st.dout, kDoutChunk, tile, row);
-      *reinterpret_cast<uint4*>(gd + brole_off(row & 63, 0, kHO)) = pack8(d16);
-      *reinterpret_cast<uint4*>(gd + brole_off(row & 63, 8, kHO)) = pack8(d16 + 8);
-#pragma unroll
-      for (int j = 0; j < kMaxOut; ++j) s_out[row][j] = d[j];
+      *reinterpret_cast<uint4*>(gd + brole_off(row & 63, 0, kHO)) = p0;
+      *reinterpret_cast<uint4*>(gd + brole_off(row & 63, 8, kHO)) = p1;
+      // dOut as the A operand of dA_4 = dOut W_h: K-major [128][16] in the A_lo region
+      *reinterpret_cast<uint4*>(sm + kOffALo + tc::kmajor_off(row, 0, 2)) = p0;
+      *reinterpret_cast<uint4*>(sm + kOffALo + tc::kmajor_off(row, 8, 2)) = p1;
       // tile partials: head-bias gradient (sum of d) and the loss, reduced over the 128 rows
       float red[kMaxOut + 1];
 #pragma unroll
@@ -413,25 +504,29 @@ __global__ void __launch_bounds__(256, 1) mlp_train_fb_kernel(const __grid_const
         s_red[warp][kHO] = red[kMaxOut];
       }
     }
-    __syncthreads();
+    tc::fence_proxy_async_smem();
+    sync_all();
+    if (tid == 0 && !s_fail)
+      if (!head_bwd(ch)) s_fail = 1;
+    ch += 1;
     if (tid < kPart) a.tile_part[(size_t)tile * kPart + tid] = s_red[0][tid] + s_red[1][tid] + s_red[2][tid] + s_red[3][tid];
+    sync_all();
+    if (s_fail) break;
 
-    // ---- dZ_3 = (dOut W_h) * SiLU'(z_3); z_3 is still in TMEM ----
+    // ---- dZ_3 = dA_4 * SiLU'(z_3); z_3 and dA_4 are in TMEM ----
     {
       unsigned char* gdz = chunk_ptr(a.st.dz[3], kDzChunk, tile, row);
 #pragma unroll 1
       for (int cb = 0; cb < 4; ++cb) {
         const int col0 = 128 * chalf + 32 * cb;
-        float v[32];
+        float v[32], da[32];
         tc::tmem_ld32(trow + col0, v);
+        tc::tmem_ld32(trow + kW + col0, da);
 #pragma unroll
         for (int i = 0; i < 32; ++i) {
           const float z = v[i] + s_bias[3][col0 + i];
           const float s = sigmoid_f(z);
-          float da = 0.f;
-#pragma unroll
-          for (int j = 0; j < kMaxOut; ++j) da = fmaf(s_out[row][j], s_wh[j][col0 + i], da);
-          v[i] = da * s * fmaf(z, 1.0f - s, 1.0f);
+          v[i] = da[i] * s * fmaf(z, 1.0f - s, 1.0f);
         }
 #pragma unroll
         for (int g8 = 0; g8 < 4; ++g8) {
@@ -447,26 +542,30 @@ __global__ void __launch_bounds__(256, 1) mlp_train_fb_kernel(const __grid_const
 
     // ---- backward: dA_l = dZ_l W_l, dZ_{l-1} = dA_l * SiLU'(z_{l-1}) ----
     for (int l = 3; l >= 1; --l) {
+      // this thread's SiLU derivatives for the epilogue, loaded while the MMAs run
+      const unsigned char* ggate = a.st.gate[l - 1] + (size_t)tile * kGateTile;
+      uint4 graw[16];
+#pragma unroll
+      for (int cb = 0; cb < 4; ++cb) {
+        const uint4* gp = reinterpret_cast<const uint4*>(ggate + ((size_t)(4 * chalf + cb) * kRows + row) * 64);
+#pragma unroll
+        for (int g8 = 0; g8 < 4; ++g8) graw[4 * cb + g8] = gp[g8];
+      }
       if (tid == 0 && !s_fail)
-        if (!gemm(ch, 4, true)) s_fail = 1;
-      ch += 4;
+        if (!gemm(ch, kP1, true)) s_fail = 1;
+      ch += kP1;
       sync_all();
       if (s_fail) break;
       unsigned char* gdz = chunk_ptr(a.st.dz[l - 1], kDzChunk, tile, row);
-      const unsigned char* ggate = a.st.gate[l - 1] + (size_t)tile * kGateTile;
-#pragma unroll 1
+#pragma unroll
       for (int cb = 0; cb < 4; ++cb) {
         const int col0 = 128 * chalf + 32 * cb;
-        const uint4* gp = reinterpret_cast<const uint4*>(ggate + ((size_t)(col0 >> 5) * kRows + row) * 64);
-        uint4 graw[4];
-#pragma unroll
-        for (int g8 = 0; g8 < 4; ++g8) graw[g8] = gp[g8];
         float v[32];
         tc::tmem_ld32(trow + col0, v);
 #pragma unroll
         for (int g8 = 0; g8 < 4; ++g8) {
           float gt[8];
-          unpack8(graw[g8], gt);
+          unpack8(graw[4 * cb + g8], gt);
 #pragma unroll
           for (int i = 0; i < 8; ++i) v[8 * g8 + i] *= gt[i];
           const int c8 = col0 + 8 * g8;
@@ -483,14 +582,14 @@ __global__ void __launch_bounds__(256, 1) mlp_train_fb_kernel(const __grid_const
   if (s_fail && tid == 0) {
     // let the copies still in flight land (bounded) before the CTA's shared memory goes away
     for (int64_t g = consumed; g < next_load; ++g) {
-      const int b = (int)(g & 1);
+      const int b = (int)(g % kBufs);
       if (!tc::mbar_wait_bounded(&mbar_full[b], ph_full[b], kWaitTries)) break;
       ph_full[b] ^= 1u;
     }
     atomicExch(a.status, FSG_ETIMEOUT);
   }
   sync_all();
-  if (warp == 0) tc::tmem_dealloc(tmem, kW);
+  if (warp == 0) tc::tmem_dealloc(tmem, 2 * kW);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -507,27 +606,31 @@ constexpr uint32_t kDwOnes = kDwStages * kDwStage;
 constexpr uint32_t kDwSmem = kDwOnes + 512 + 1024;
 constexpr int kDwJobs = 10;
 
+// The CTAs of the weight-gradient launch: CTAs [off[j], off[j + 1]) split job j's rows, n_split
+// CTAs per job.  A CTA's time is set by its number of 64-row chunks (each chunk's copy has to
+// arrive from the stash, which does not stay in L2), so every job gets the same split.
+struct SplitMap {
+  int off[kDwJobs + 1];
+};
+
+__host__ __device__ inline SplitMap split_map(int n_split) {
+  SplitMap m;
+  m.off[0] = 0;
+  for (int j = 0; j < kDwJobs; ++j) {
+    const int n = n_split;
+    m.off[j + 1] = m.off[j] + n;
+  }
+  return m;
+}
+
 struct DwArgs {
   Stash st;
   int n_chunks;            // 64-row chunks in the batch
-  int n_split;
-  float* dw_part;          // [job][split][128][256]
-  float* db_part;          // [job][split][128]
+  SplitMap map;
+  float* dw_part;          // [CTA][128][256]
+  float* db_part;          // [CTA][128]
   int* status;
 };
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-      "%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
 
 __global__ void __launch_bounds__(128, 1) mlp_train_dw_kernel(const __grid_constant__ DwArgs a) {
   extern __shared__ __align__(1024) unsigned char sm[];
@@ -535,7 +638,9 @@ __global__ void __launch_bounds__(128, 1) mlp_train_dw_kernel(const __grid_const
   __shared__ uint32_t tmem_holder;
   __shared__ int s_fail;
   const int tid = threadIdx.x, warp = tid >> 5;
-  const int job = blockIdx.x / a.n_split, split = blockIdx.x % a.n_split;
+  int job = 0;
+  while (job + 1 < kDwJobs && (int)blockIdx.x >= a.map.off[job + 1]) ++job;
+  const int split = (int)blockIdx.x - a.map.off[job], n_split = a.map.off[job + 1] - a.map.off[job];
   const bool head = job >= 8;
   const int layer = head ? 4 : job / 2, half = head ? job - 8 : job % 2;
   const int wd = head ? kHO : (layer == 0 ? kFeat : kW);
@@ -543,8 +648,8 @@ __global__ void __launch_bounds__(128, 1) mlp_train_dw_kernel(const __grid_const
   const unsigned char* hsrc = head ? a.st.dout : a.st.act[layer];
   const size_t g_chunk = kDzChunk;  // A-role tensors are 256 wide
   const size_t h_chunk = (size_t)64 * wd * 2;
-  const int c0 = (int)((int64_t)split * a.n_chunks / a.n_split);
-  const int c1 = (int)((int64_t)(split + 1) * a.n_chunks / a.n_split);
+  const int c0 = (int)((int64_t)split * a.n_chunks / n_split);
+  const int c1 = (int)((int64_t)(split + 1) * a.n_chunks / n_split);
 
   if (tid == 0) {
     for (int s = 0; s < kDwStages; ++s) {
@@ -580,10 +685,21 @@ __global__ void __launch_bounds__(128, 1) mlp_train_dw_kernel(const __grid_const
     uint32_t ph_full[kDwStages] = {}, ph_free[kDwStages] = {};
     bool ok = true;
     int next = 0, consumed = 0;
-    auto issue = [&](int i) -> bool {
+    // Copies chunk i into stage i % kDwStages once the stage's previous chunk is released by its
+    // MMAs: blocking (bounded; `failed` on timeout) or, for look-ahead copies, only if the release
+    // has already happened, so the MMAs of consecutive chunks stay queued back to back.
+    bool failed = false;
+    auto issue = [&](int i, bool block) -> bool {
       const int s = i % kDwStages;
       if (i >= kDwStages) {
-        if (!tc::mbar_wait_bounded(&mbar_free[s], ph_free[s], kWaitTries)) return false;
+        if (block) {
+          if (!tc::mbar_wait_bounded(&mbar_free[s], ph_free[s], kWaitTries)) {
+            failed = true;
+            return false;
+          }
+        } else if (!tc::mbar_test(&mbar_free[s], ph_free[s])) {
+          return false;
+        }
         ph_free[s] ^= 1u;
       }
       unsigned char* dst = sm + s * kDwStage;
@@ -594,8 +710,11 @@ __global__ void __launch_bounds__(128, 1) mlp_train_dw_kernel(const __grid_const
       return true;
     };
     for (int i = 0; i < n && ok; ++i) {
-      while (ok && next < n && next < i + kDwStages) ok = issue(next++);
-      if (!ok) break;
+      while (next < n && next < i + kDwStages) {
+        if (!issue(next, next <= i)) break;
+        ++next;
+      }
+      if (failed) { ok = false; break; }
       const int s = i % kDwStages;
       if (!tc::mbar_wait_bounded(&mbar_full[s], ph_full[s], kWaitTries)) { ok = false; break; }
       ph_full[s] ^= 1u;
@@ -629,7 +748,7 @@ __global__ void __launch_bounds__(128, 1) mlp_train_dw_kernel(const __grid_const
   __syncthreads();
   tc::fence_after_sync();
   const int m = 32 * warp + (tid & 31);  // TMEM lane = output row of this half
-  float* out = a.dw_part + (((size_t)job * a.n_split + split) * 128 + m) * 256;
+  float* out = a.dw_part + ((size_t)blockIdx.x * 128 + m) * 256;
   const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
   if (!s_fail) {
     if (c1 > c0) {
@@ -642,11 +761,11 @@ __global__ void __launch_bounds__(128, 1) mlp_train_dw_kernel(const __grid_const
       if (!head) {
         float v[16];
         tmem_ld16(trow + 256, v);
-        a.db_part[((size_t)job * a.n_split + split) * 128 + m] = v[0];
+        a.db_part[(size_t)blockIdx.x * 128 + m] = v[0];
       }
     } else {  // an empty split contributes zeros
       for (int c = 0; c < wd; ++c) out[c] = 0.f;
-      if (!head) a.db_part[((size_t)job * a.n_split + split) * 128 + m] = 0.f;
+      if (!head) a.db_part[(size_t)blockIdx.x * 128 + m] = 0.f;
     }
   }
   tc::fence_before_sync();
@@ -670,13 +789,15 @@ struct AdamArgs {
   float* wh;
   float* mwh;
   float* vwh;
+  void* head_packed;
   float* bh;
   float* mbh;
   float* vbh;
   const float* dw_part;
   const float* db_part;
   const float* tile_part;
-  int n_split, n_tiles, n_out;
+  SplitMap map;
+  int n_tiles, n_out;
   int* step;
   float* loss_hist;
   int hist_len;
@@ -692,15 +813,22 @@ __host__ __device__ inline int64_t n_params(int n_out) {
   return (int64_t)kW * kFeat + 3LL * kW * kW + 4LL * kW + (int64_t)n_out * kW + n_out;
 }
 
+__device__ __forceinline__ float adam_step(float g, float w, float& m1, float& m2, float lr, float b1, float b2,
+                                           float eps, float bc1, float bc2) {
+  m1 = b1 * m1 + (1.f - b1) * g;
+  m2 = b2 * m2 + (1.f - b2) * g * g;
+  return w - lr * (m1 / bc1) / (sqrtf(m2 / bc2) + eps);
+}
+
+// One thread per parameter: the gradient is the fixed-order sum of its job's split partials.
 __global__ void __launch_bounds__(256) mlp_train_adam_kernel(const __grid_constant__ AdamArgs a) {
   const int64_t total = n_params(a.n_out);
   const int t = *reinterpret_cast<volatile const int*>(a.step);  // advanced only by the last block
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p < total) {
-    const int ns = a.n_split;
     float g = 0.f;
     float *w, *m1, *m2;
-    int layer = -1, mrow = 0, ncol = 0;
+    int layer = -1, mrow = 0, ncol = 0, hj = -1, hk = 0;
     const int64_t nw0 = (int64_t)kW * kFeat, nw = (int64_t)kW * kW;
     const int64_t off_b = nw0 + 3 * nw, off_h = off_b + 4 * kW, off_bh = off_h + (int64_t)a.n_out * kW;
     if (p < off_b) {
@@ -710,18 +838,24 @@ __global__ void __launch_bounds__(256) mlp_train_adam_kernel(const __grid_consta
       mrow = (int)(q / K);
       ncol = (int)(q % K);
       const int job = 2 * layer + mrow / 128;
-      for (int s = 0; s < ns; ++s) g += a.dw_part[(((size_t)job * ns + s) * 128 + (mrow & 127)) * 256 + ncol];
+#pragma unroll 8
+      for (int s = a.map.off[job]; s < a.map.off[job + 1]; ++s)
+        g += a.dw_part[((size_t)s * 128 + (mrow & 127)) * 256 + ncol];
       w = a.w[layer] + q; m1 = a.mw[layer] + q; m2 = a.vw[layer] + q;
     } else if (p < off_h) {
       const int l = (int)((p - off_b) / kW), mm = (int)((p - off_b) % kW);
       const int job = 2 * l + mm / 128;
-      for (int s = 0; s < ns; ++s) g += a.db_part[((size_t)job * ns + s) * 128 + (mm & 127)];
+#pragma unroll 8
+      for (int s = a.map.off[job]; s < a.map.off[job + 1]; ++s) g += a.db_part[(size_t)s * 128 + (mm & 127)];
       w = a.b[l] + mm; m1 = a.mb[l] + mm; m2 = a.vb[l] + mm;
     } else if (p < off_bh) {
       const int64_t q = p - off_h;
-      const int j = (int)(q / kW), k = (int)(q % kW);
-      const int job = 8 + k / 128;
-      for (int s = 0; s < ns; ++s) g += a.dw_part[(((size_t)job * ns + s) * 128 + (k & 127)) * 256 + j];
+      hj = (int)(q / kW);
+      hk = (int)(q % kW);
+      const int job = 8 + hk / 128;
+#pragma unroll 8
+      for (int s = a.map.off[job]; s < a.map.off[job + 1]; ++s)
+        g += a.dw_part[((size_t)s * 128 + (hk & 127)) * 256 + hj];
       w = a.wh + q; m1 = a.mwh + q; m2 = a.vwh + q;
     } else {
       const int j = (int)(p - off_bh);
@@ -733,22 +867,28 @@ __global__ void __launch_bounds__(256) mlp_train_adam_kernel(const __grid_consta
       const int tt = t + 1;
       float lr;
       if (tt <= a.warmup) {
-        lr = a.lr * (float)tt / (float)a.warmup;
+        lr = a.lr * (float)tt / (float)max(1, a.warmup);
       } else {
         const float prog = fminf(1.0f, (float)(tt - a.warmup) / (float)max(1, a.total_steps - a.warmup));
         lr = a.lr_min + (a.lr - a.lr_min) * 0.5f * (1.0f + cospif(prog));
       }
       const float bc1 = 1.0f - powf(a.b1, (float)tt), bc2 = 1.0f - powf(a.b2, (float)tt);
-      const float mv = a.b1 * *m1 + (1.f - a.b1) * g;
-      const float vv = a.b2 * *m2 + (1.f - a.b2) * g * g;
+      float mv = *m1, vv = *m2;
+      const float nwv = adam_step(g, *w, mv, vv, lr, a.b1, a.b2, a.eps, bc1, bc2);
       *m1 = mv;
       *m2 = vv;
-      const float nwv = *w - lr * (mv / bc1) / (sqrtf(vv / bc2) + a.eps);
       *w = nwv;
+      if (hj >= 0) {  // the head's packed chunk: hi and lo (forward), hi (backward)
+        const __nv_bfloat16 hi = __float2bfloat16_rn(nwv);
+        __nv_bfloat16* o = static_cast<__nv_bfloat16*>(a.head_packed);
+        o[(kHeadHi + tc::kmajor_off(hj, hk, kW / 8)) / 2] = hi;
+        o[(kHeadLo + tc::kmajor_off(hj, hk, kW / 8)) / 2] = __float2bfloat16_rn(nwv - __bfloat162float(hi));
+        o[(kHeadBwd + tc::mnmajor_off(hk, hj, kW / 8)) / 2] = hi;
+      }
       if (layer >= 0) {
         const __nv_bfloat16 hb = __float2bfloat16_rn(nwv);
         __nv_bfloat16* f = static_cast<__nv_bfloat16*>(a.wf[layer]);
-        f[(size_t)(ncol / kChunkK) * (kChunkBytes / 2) + tc::kmajor_off(mrow, ncol % kChunkK, kChunkK / 8) / 2] = hb;
+        f[(size_t)(ncol / kChunkK) * (kChunkBytes / 2) + wpack_off(mrow, ncol % kChunkK) / 2] = hb;
         if (layer > 0) {
           __nv_bfloat16* b = static_cast<__nv_bfloat16*>(a.wb[layer]);
           b[(size_t)(mrow / kChunkK) * (kChunkBytes / 2) + tc::mnmajor_off(ncol, mrow % kChunkK, kW / 8) / 2] = hb;
@@ -775,13 +915,29 @@ __global__ void __launch_bounds__(256) mlp_train_adam_kernel(const __grid_consta
 }
 
 // Writes the packed BF16 copies of hidden layer l from its FP32 master weights.
+// Writes the packed head chunk: entry (region r, output j, feature k) of W_h, zero for j >= n_out.
+__global__ void mlp_train_pack_head_kernel(const float* __restrict__ wh, int n_out, void* packed) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 3 * kHO * kW) return;
+  const int r = t / (kHO * kW), j = (t / kW) % kHO, k = t % kW;
+  float v = 0.f;
+  if (j < n_out) {
+    const float w = wh[j * kW + k];
+    const __nv_bfloat16 hi = __float2bfloat16_rn(w);
+    v = r == 1 ? w - __bfloat162float(hi) : w;
+  }
+  __nv_bfloat16* o = static_cast<__nv_bfloat16*>(packed);
+  const uint32_t off = r == 2 ? kHeadBwd + tc::mnmajor_off(k, j, kW / 8) : (r ? kHeadLo : kHeadHi) + tc::kmajor_off(j, k, kW / 8);
+  o[off / 2] = __float2bfloat16_rn(v);
+}
+
 __global__ void mlp_train_pack_kernel(const float* __restrict__ w, int layer, void* wf, void* wb) {
   const int K = layer == 0 ? kFeat : kW;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= kW * K) return;
   const int m = i / K, n = i % K;
   const __nv_bfloat16 hb = __float2bfloat16_rn(w[i]);
-  static_cast<__nv_bfloat16*>(wf)[(size_t)(n / kChunkK) * (kChunkBytes / 2) + tc::kmajor_off(m, n % kChunkK, 8) / 2] = hb;
+  static_cast<__nv_bfloat16*>(wf)[(size_t)(n / kChunkK) * (kChunkBytes / 2) + wpack_off(m, n % kChunkK) / 2] = hb;
   if (layer > 0 && wb)
     static_cast<__nv_bfloat16*>(wb)[(size_t)(m / kChunkK) * (kChunkBytes / 2) + tc::mnmajor_off(n, m % kChunkK, 32) / 2] =
         hb;
@@ -824,8 +980,8 @@ Stash carve_stash(unsigned char* base, int n_tiles) {
 }
 
 size_t part_bytes(int n_split, int n_tiles) {
-  return (size_t)kDwJobs * n_split * 128 * 256 * 4 + (size_t)kDwJobs * n_split * 128 * 4 + (size_t)n_tiles * kPart * 4 +
-         256;
+  const size_t ctas = (size_t)split_map(n_split).off[kDwJobs];
+  return ctas * 128 * 256 * 4 + ctas * 128 * 4 + (size_t)n_tiles * kPart * 4 + 256;
 }
 
 int validate_train(const FsgMlpTrain* t) {
@@ -839,7 +995,8 @@ int validate_train(const FsgMlpTrain* t) {
     if (!t->w[l] || !t->m_w[l] || !t->v_w[l] || !t->packed_fwd[l] || !t->b[l] || !t->m_b[l] || !t->v_b[l] ||
         (l > 0 && !t->packed_bwd[l]))
       return set_error(FSG_EINVAL, "layer %d parameters missing", l);
-  if (!t->w_head || !t->m_w_head || !t->v_w_head || !t->b_head || !t->m_b_head || !t->v_b_head || !t->bmat)
+  if (!t->w_head || !t->m_w_head || !t->v_w_head || !t->b_head || !t->m_b_head || !t->v_b_head || !t->bmat ||
+      !t->packed_head)
     return set_error(FSG_EINVAL, "head or feature parameters missing");
   if (!t->step || !t->status || !t->workspace) return set_error(FSG_EINVAL, "step counter, status or workspace missing");
   if (t->workspace_bytes < fsg_mlp_train_workspace_size(t->n_tiles, t->n_split))
@@ -865,8 +1022,10 @@ int launch_step(const FsgMlpTrain* t, int apply, float* grads_out, int* rows_out
   Stash st = carve_stash(ws, t->n_tiles);
   unsigned char* pb = ws + stash_bytes_for(t->n_tiles);
   float* dw_part = reinterpret_cast<float*>(pb);
-  float* db_part = dw_part + (size_t)kDwJobs * t->n_split * 128 * 256;
-  float* tile_part = db_part + (size_t)kDwJobs * t->n_split * 128;
+  const SplitMap map = split_map(t->n_split);
+  const int dw_ctas = map.off[kDwJobs];
+  float* db_part = dw_part + (size_t)dw_ctas * 128 * 256;
+  float* tile_part = db_part + (size_t)dw_ctas * 128;
   unsigned int* done = reinterpret_cast<unsigned int*>(tile_part + (size_t)t->n_tiles * kPart);
 
   FbArgs fa;
@@ -881,7 +1040,7 @@ int launch_step(const FsgMlpTrain* t, int apply, float* grads_out, int* rows_out
     fa.net.wb[l] = t->packed_bwd[l];
     fa.net.bias[l] = t->b[l];
   }
-  fa.net.whead = t->w_head;
+  fa.net.whead = t->packed_head;
   fa.net.bhead = t->b_head;
   fa.net.n_out = t->n_out;
   fa.inv_batch = 1.0f / (float)(t->n_tiles * kRows);
@@ -898,11 +1057,11 @@ int launch_step(const FsgMlpTrain* t, int apply, float* grads_out, int* rows_out
   DwArgs da;
   da.st = st;
   da.n_chunks = t->n_tiles * 2;
-  da.n_split = t->n_split;
+  da.map = map;
   da.dw_part = dw_part;
   da.db_part = db_part;
   da.status = t->status;
-  mlp_train_dw_kernel<<<kDwJobs * t->n_split, 128, kDwSmem, s>>>(da);
+  mlp_train_dw_kernel<<<dw_ctas, 128, kDwSmem, s>>>(da);
   if ((st_ = check_cuda(cudaGetLastError(), "mlp_train_dw_kernel launch")) != FSG_OK) return st_;
 
   AdamArgs aa;
@@ -919,13 +1078,14 @@ int launch_step(const FsgMlpTrain* t, int apply, float* grads_out, int* rows_out
   aa.wh = t->w_head;
   aa.mwh = t->m_w_head;
   aa.vwh = t->v_w_head;
+  aa.head_packed = t->packed_head;
   aa.bh = t->b_head;
   aa.mbh = t->m_b_head;
   aa.vbh = t->v_b_head;
   aa.dw_part = dw_part;
   aa.db_part = db_part;
   aa.tile_part = tile_part;
-  aa.n_split = t->n_split;
+  aa.map = map;
   aa.n_tiles = t->n_tiles;
   aa.n_out = t->n_out;
   aa.step = t->step;
@@ -965,6 +1125,8 @@ extern "C" int32_t fsg_mlp_train_init(const FsgMlpTrain* t, void* stream) {
     mlp_train_pack_kernel<<<(kW * K + 255) / 256, 256, 0, s>>>(t->w[l], l, t->packed_fwd[l], t->packed_bwd[l]);
     if ((st = check_cuda(cudaGetLastError(), "mlp_train_pack_kernel launch")) != FSG_OK) return st;
   }
+  mlp_train_pack_head_kernel<<<(3 * kHO * kW + 255) / 256, 256, 0, s>>>(t->w_head, t->n_out, t->packed_head);
+  if ((st = check_cuda(cudaGetLastError(), "mlp_train_pack_head_kernel launch")) != FSG_OK) return st;
   unsigned char* ws = static_cast<unsigned char*>(t->workspace);
   unsigned char* done = ws + fsg_mlp_train_workspace_size(t->n_tiles, t->n_split) - 256;
   return check_cuda(cudaMemsetAsync(done, 0, 256, s), "training counter reset");

@@ -99,6 +99,7 @@ class TxFieldSurrogate:
                            for w in self.W[:DEPTH]]
         self.packed_bwd = [None] + [torch.empty(HIDDEN * HIDDEN * 2, dtype=torch.uint8, device=dev)
                                     for _ in range(DEPTH - 1)]
+        self.packed_head = torch.zeros(24576, dtype=torch.uint8, device=dev)  # W_head, BF16 hi/lo + MN-major hi
         self.step_counter = torch.zeros(1, dtype=torch.int32, device=dev)
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.scale = 1.0
@@ -193,6 +194,7 @@ class TxFieldSurrogate:
                                             self.vW[DEPTH].data_ptr())
         t.b_head, t.m_b_head, t.v_b_head = (self.b[DEPTH].data_ptr(), self.mb[DEPTH].data_ptr(),
                                             self.vb[DEPTH].data_ptr())
+        t.packed_head = self.packed_head.data_ptr()
         t.n_out, t.n_tiles, t.n_split = self.n_out, int(n_tiles), int(n_split)
         t.total_steps, t.warmup_steps = int(total_steps), int(warmup)
         t.lr, t.lr_min, t.beta1, t.beta2, t.eps = float(lr), float(lr_min), 0.9, 0.999, 1e-8

@@ -266,8 +266,8 @@ int32_t fsg_surrogate_combine(const FsgSurrogateDomain* dom, const double* sampl
  * and the loss history live on the device, so a sequence of steps needs no host
  * synchronisation and can be captured in a CUDA graph.  All pointers are device memory owned
  * by the caller.  packed_fwd[l]: fsg_mlp_tc_packed_bytes(K) bytes (the layout of
- * fsg_mlp_tc_pack); packed_bwd[1..3]: 128 KB each.  fsg_mlp_train_init writes both packed
- * copies from the FP32 weights and clears the workspace counters.
+ * fsg_mlp_tc_pack); packed_bwd[1..3]: 128 KB each; packed_head: 24 KB.  fsg_mlp_train_init
+ * writes the packed copies from the FP32 weights and clears the workspace counters.
  */
 typedef struct FsgMlpTrain {
   const float* u;                 /* [n_data][4] */
@@ -289,9 +289,11 @@ typedef struct FsgMlpTrain {
   float* b_head;                  /* [n_out] */
   float* m_b_head;
   float* v_b_head;
+  void* packed_head;              /* 24 KB: W_head as BF16 hi + lo (forward) and hi (backward) */
   int32_t n_out;                  /* 2 n_carriers, <= 10 */
   int32_t n_tiles;                /* batch = 128 n_tiles rows */
-  int32_t n_split;                /* row splits of the weight-gradient kernel */
+  int32_t n_split;                /* weight-gradient CTAs per (layer, output half) job; 10 jobs
+                                     (15 fills 150 of 152 SMs) */
   int32_t total_steps;
   int32_t warmup_steps;
   float lr, lr_min, beta1, beta2, eps;
