@@ -155,7 +155,14 @@ __global__ void __launch_bounds__(256, 1) mlp_tc_forward_kernel(const __grid_con
         for (int c = 0; c < nch && ok; ++c) {
           const int64_t g = chunk0 + c;
           const int b = (int)(g & 1);
-          while (ok && next_load < g + 2 && next_load < total_chunks) ok = load(next_load++);
+          // the look-ahead copy (chunk g + 1) reuses chunk g - 1's buffer: issue it only if that
+          // chunk's MMAs are done, so that the MMAs of consecutive chunks stay queued back to back
+          while (ok && next_load < g + 2 && next_load < total_chunks) {
+            if (next_load > g && next_load >= 2 &&
+                !tc::mbar_test(&mbar_free[next_load & 1], ph_free[next_load & 1]))
+              break;
+            ok = load(next_load++);
+          }
           if (!ok) break;
           if (!tc::mbar_wait_bounded(&mbar_full[b], ph_full[b], kMlpWaitTries)) { ok = false; break; }
           ph_full[b] ^= 1u;

@@ -484,3 +484,39 @@ def cfg5_box(params: TransducerParams) -> Box:
                max_angle=16.0 * math.pi / 180.0)
 
 
+
+
+def main(argv=None):
+    """Train the surrogate of the 64-element probe over its training box and print the report:
+    ``python -m fastsimus_gb300.surrogate [--steps N] [--n-train M] [--block B] [--seed S]``."""
+    import argparse
+    import json
+
+    from fastsimus_gb300 import workloads as W
+
+    ap = argparse.ArgumentParser(description=main.__doc__)
+    ap.add_argument("--steps", type=int, default=60_000)
+    ap.add_argument("--n-train", type=int, default=2_000_000)
+    ap.add_argument("--block", type=int, default=1000, help="steps per CUDA-graph replay")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--predict", type=int, default=0, help="then time inference on this many queries")
+    a = ap.parse_args(argv)
+    p, m = W.cfg1_probe(), W.cfg1_medium()
+    sur = TxFieldSurrogate(p, m, cfg5_box(p), seed=a.seed)
+    rep = sur.train(n_train=a.n_train, steps=a.steps, block=a.block, seed=a.seed, evals=1)
+    out = {k: v for k, v in rep.items() if k != "loss_curve"}
+    if a.predict:
+        q = sur.sample_domain(a.predict, seed=a.seed + 9)
+        sur.predict(q)
+        torch.cuda.synchronize(sur.device)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        sur.predict(q)
+        e1.record()
+        torch.cuda.synchronize(sur.device)
+        out["predict_ns_per_query"] = e0.elapsed_time(e1) * 1e6 / a.predict
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()
