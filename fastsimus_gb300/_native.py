@@ -17,7 +17,7 @@ LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libfsgb300.so"
 FSG_OK, FSG_EINVAL, FSG_ECUDA, FSG_ETIMEOUT, FSG_EUNSUPPORTED, FSG_EWORKSPACE = range(6)
 FSG_BAFFLE_SOFT, FSG_BAFFLE_RIGID, FSG_BAFFLE_IMPEDANCE = range(3)
 FSG_OUT_SELECTED_RAW, FSG_OUT_FULL_CORRECTED = range(2)
-ABI_VERSION = 2
+ABI_VERSION = 3
 
 
 class FsgError(RuntimeError):
@@ -112,11 +112,12 @@ _SIGNATURES = {
     "fsg_pfield": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgMedium), ctypes.POINTER(FsgFreqPlan),
                                     _P, ctypes.c_int64, _P, _P, ctypes.c_int32, _P, _P, ctypes.c_size_t, _P]),
     "fsg_simus_batched_workspace_size": (ctypes.c_size_t, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgPhantom),
-                                                           ctypes.c_int32, ctypes.c_int32,
+                                                           ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                                            ctypes.POINTER(FsgBatchTuning)]),
     "fsg_simus_batched": (ctypes.c_int32, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgMedium),
                                            ctypes.POINTER(FsgPhantom), ctypes.c_int32, _P, _P, ctypes.c_int32,
-                                           ctypes.POINTER(FsgBatchTuning), _P, ctypes.c_size_t, _P]),
+                                           ctypes.c_int32, ctypes.POINTER(FsgBatchTuning), _P, ctypes.c_size_t,
+                                           _P]),
     "fsg_simus_batched_tc_workspace_size": (ctypes.c_size_t, [ctypes.POINTER(FsgProbe), ctypes.POINTER(FsgPhantom),
                                                               ctypes.c_int32, ctypes.c_int32,
                                                               ctypes.POINTER(FsgBatchTuning)]),

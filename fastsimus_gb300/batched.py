@@ -60,10 +60,16 @@ class BatchedSimus:
 
     def __init__(self, phantoms, delays, params: TransducerParams, medium: MediumParams = _DEFAULT_MEDIUM, *,
                  plans: list[SimusPlan] | None = None, tx_apodization=None, tuning: BatchTuning | None = None,
-                 fs: float | None = None, device: torch.device | None = None, backend: str = "fp32"):
+                 fs: float | None = None, device: torch.device | None = None, backend: str = "fp32",
+                 full_frequency_directivity: bool = False):
         if backend not in ("fp32", "tc"):
             raise ValueError("backend must be 'fp32' (CUDA cores) or 'tc' (tcgen05 BF16 hi/lo tensor cores)")
+        if full_frequency_directivity and backend == "tc":
+            raise NotImplementedError("full_frequency_directivity is implemented by the fp32 batched backend "
+                                      "(and fsg_simus); the tensor-core backend uses the centre-frequency "
+                                      "directivity")
         self.backend = backend
+        self.ffd = bool(full_frequency_directivity)
         self.device = device or _device.require_cuda()
         self.lib = _native.load()
         self.params, self.medium = params, medium
@@ -86,7 +92,7 @@ class BatchedSimus:
         self.apod = None
         if tx_apodization is not None:
             a = np.broadcast_to(np.asarray(tx_apodization, dtype=np.float64), d.shape)
-            self.apod = torch.as_tensor(np.ascontiguousarray(a), device=self.device)
+            self.apod = torch.as_tensor(np.array(a, dtype=np.float64, copy=True), device=self.device)
         self.tabs = [_device.plan_tables(p, self.device) for p in plans]
         self.outs = [torch.empty((self.n_tx, p.n_freq_full, params.n_elements), dtype=torch.complex64,
                                  device=self.device) for p in plans]
@@ -111,9 +117,12 @@ class BatchedSimus:
     def set_tuning(self, tuning: BatchTuning):
         self.tuning = tuning
         self._ph = self._fsg_phantoms()
-        size_fn = (self.lib.fsg_simus_batched_tc_workspace_size if self.backend == "tc"
-                   else self.lib.fsg_simus_batched_workspace_size)
-        nbytes = size_fn(self.probe, self._ph, len(self.phantoms), self.n_tx, tuning.to_c())
+        if self.backend == "tc":
+            nbytes = self.lib.fsg_simus_batched_tc_workspace_size(self.probe, self._ph, len(self.phantoms), self.n_tx,
+                                                                  tuning.to_c())
+        else:
+            nbytes = self.lib.fsg_simus_batched_workspace_size(self.probe, self._ph, len(self.phantoms), self.n_tx,
+                                                               int(self.ffd), tuning.to_c())
         if nbytes == 0:
             raise ValueError("fsg_simus_batched_workspace_size rejected the batch")
         self.ws = _device.workspace(nbytes, self.device)
@@ -121,12 +130,18 @@ class BatchedSimus:
 
     def launch_sweep(self):
         """Enqueue the batched sweep on the current stream (outputs: corrected spectra)."""
-        fn = self.lib.fsg_simus_batched_tc if self.backend == "tc" else self.lib.fsg_simus_batched
+        apod = self.apod.data_ptr() if self.apod is not None else None
         with torch.cuda.device(self.device), _device.timed("fsg_simus_batched", self.device):
-            st = fn(self.probe, self.med, self._ph, len(self.phantoms),
-                                            self.delays.data_ptr(), self.apod.data_ptr() if self.apod is not None
-                                            else None, self.n_tx, self.tuning.to_c(), self.ws.data_ptr(),
-                                            self.ws.numel(), _device.stream_handle(self.device))
+            if self.backend == "tc":
+                st = self.lib.fsg_simus_batched_tc(self.probe, self.med, self._ph, len(self.phantoms),
+                                                   self.delays.data_ptr(), apod, self.n_tx, self.tuning.to_c(),
+                                                   self.ws.data_ptr(), self.ws.numel(),
+                                                   _device.stream_handle(self.device))
+            else:
+                st = self.lib.fsg_simus_batched(self.probe, self.med, self._ph, len(self.phantoms),
+                                                self.delays.data_ptr(), apod, self.n_tx, int(self.ffd),
+                                                self.tuning.to_c(), self.ws.data_ptr(), self.ws.numel(),
+                                                _device.stream_handle(self.device))
         _native.check(st)
 
     def device_status(self) -> int:
@@ -239,7 +254,8 @@ class BatchedSimus:
     def _tune_key(self) -> str:
         total = sum(int(s.shape[0]) for s, _ in self.phantoms)
         fbar = int(np.mean([p.selected_freqs.shape[0] for p in self.plans]))
-        return (f"{self.backend}-E{self.params.n_elements}-U{self.plans[0].n_sub}-T{self.n_tx}-P{len(self.phantoms)}"
+        return (f"{self.backend}{'-ffd' if self.ffd else ''}-E{self.params.n_elements}-U{self.plans[0].n_sub}"
+                f"-T{self.n_tx}-P{len(self.phantoms)}"
                 f"-S{int(np.log2(max(total, 1)))}-F{fbar // 64}")
 
 
@@ -275,9 +291,11 @@ def _save_cache(table: dict):
 
 def simus_batched(phantoms, delays, params: TransducerParams, medium: MediumParams = _DEFAULT_MEDIUM, *,
                   plans: list[SimusPlan] | None = None, tx_apodization=None, fs: float | None = None,
-                  tuning: BatchTuning | None = None, backend: str = "fp32") -> list[SimusResult]:
+                  tuning: BatchTuning | None = None, backend: str = "fp32",
+                  full_frequency_directivity: bool = False) -> list[SimusResult]:
     """RF of every (phantom, firing): ``phantoms`` is a list of (scatterers (S, 2), rc (S,)),
     ``delays`` is (n_tx, n_elements).  Returns per phantom rf (n_samples, E, n_tx) float32 and
     spectrum (n_freq_full, E, n_tx) complex64, on the GPU."""
     return BatchedSimus(phantoms, delays, params, medium, plans=plans, tx_apodization=tx_apodization,
-                        tuning=tuning, fs=fs, backend=backend).run()
+                        tuning=tuning, fs=fs, backend=backend,
+                        full_frequency_directivity=full_frequency_directivity).run()

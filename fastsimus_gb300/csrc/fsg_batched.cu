@@ -8,7 +8,9 @@
 //     TX:  P[s][t]  = sum_e Gm[s][e] * D[e][t]      (D = apod * exp(i 2 pi f tau_t,e))
 //     RX:  Y[e][t] += sum_s Gm[s][e] * W[s][t]      (W = rc_s * pulse * probe * P)
 // with Gm = mean_u G(s, e, u, f) generated in shared memory from the exact double-float
-// anchor of each band.  Y for the CTA's band (1 or 2 frequencies) stays in registers across
+// anchor of each band.  With full-frequency directivity every term is weighted at its own
+// frequency by sinc(k_f half_seg sin(theta)) (_simus_strategies.py:59-62), from half_seg
+// sin(theta) cached per (scatterer, source) beside the rest of the geometry.  Y for the CTA's band (1 or 2 frequencies) stays in registers across
 // all scatterer tiles of the work item.
 //
 // Persistent launch: one CTA per SM (x blocks_per_sm) pulls work items
@@ -111,6 +113,7 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
     for (int f = 0; f < FB; ++f) pp[f] = (f < nf) ? P.pp[f0 + f] : make_float2(0.f, 0.f);
     const float2 k0 = P.kf[f0];
     const float a0 = P.af[f0];
+    const float kb0 = k0.x, kb1 = (f0 + 1 < P.n_freq) ? P.kf[f0 + 1].x : 0.f;  // FP32 k_f for the directivity
     SweepConst C = A.C;  // probe constants; the recurrence step belongs to this phantom's plan
     C.dk = P.dk;
     C.dalpha = P.dalpha;
@@ -152,8 +155,19 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
             for (int u = 0; u < U; ++u) {
               const float4 ga = A.geo_a[rec + u];
               const float2 a = anchor_value(ga.x, ga.y, ga.z, k0, a0);
-              g0 = cadd(g0, a);
-              if (FB > 1) g1 = cadd(g1, cmul(a, make_float2(ga.w, A.geo_b[rec + u])));
+              if (A.geo_c) {
+                const float x = A.geo_c[rec + u];
+                const float d0 = sinc_poly(kb0 * x);
+                g0 = make_float2(fmaf(a.x, d0, g0.x), fmaf(a.y, d0, g0.y));
+                if (FB > 1) {
+                  const float2 a1 = cmul(a, make_float2(ga.w, A.geo_b[rec + u]));
+                  const float d1 = sinc_poly(kb1 * x);
+                  g1 = make_float2(fmaf(a1.x, d1, g1.x), fmaf(a1.y, d1, g1.y));
+                }
+              } else {
+                g0 = cadd(g0, a);
+                if (FB > 1) g1 = cadd(g1, cmul(a, make_float2(ga.w, A.geo_b[rec + u])));
+              }
             }
           }
           Gm[sl * kGmPitch + e] = g0;
@@ -320,6 +334,7 @@ __global__ void __launch_bounds__(kThreads) batched_geometry_kernel(const __grid
       const int64_t rec = (P.geo0 + s) * (int64_t)n_src + src;
       A.geo_a[rec] = make_float4(g.r_hi, g.r_lo, g.amp, g.step.x);
       A.geo_b[rec] = g.step.y;
+      if (A.geo_c) A.geo_c[rec] = C.half_seg * g.sth;
     }
   }
 }
@@ -361,11 +376,11 @@ struct BatchPlanLayout {
   int n_bands[kMaxPhantoms], n_chunks[kMaxPhantoms], item0[kMaxPhantoms];
   int64_t geo0[kMaxPhantoms], max_scat;
   size_t off_src, off_rot, off_tau, off_apod, off_queue, off_tab[kMaxPhantoms], off_partial, off_geo_a, off_geo_b,
-      total;
+      off_geo_c, total;
 };
 
 int plan_layout(const FsgProbe* probe, const FsgPhantom* ph, int n_ph, int n_tx, const FsgBatchTuning* tu,
-                BatchPlanLayout* L) {
+                BatchPlanLayout* L, int ffd = 0) {
   L->eb = batched_pad_elements(probe->n_elements);
   // two frequencies per item only fit the 64-element tile's shared memory
   L->fb = (L->eb > 64 || (tu && tu->freqs_per_item == 1)) ? 1 : 2;
@@ -401,6 +416,8 @@ int plan_layout(const FsgProbe* probe, const FsgPhantom* ph, int n_ph, int n_tx,
   o += a256((size_t)scat * E * U * 16);
   L->off_geo_b = o;
   o += a256((size_t)scat * E * U * 4);
+  L->off_geo_c = o;
+  if (ffd) o += a256((size_t)scat * E * U * 4);
   L->total = o;
   return FSG_OK;
 }
@@ -432,21 +449,37 @@ int validate_batch(const FsgProbe* probe, const FsgMedium* medium, const FsgPhan
 }  // namespace
 
 extern "C" size_t fsg_simus_batched_workspace_size(const FsgProbe* probe, const FsgPhantom* phantoms,
-                                                   int32_t n_phantoms, int32_t n_tx, const FsgBatchTuning* tuning) {
+                                                   int32_t n_phantoms, int32_t n_tx,
+                                                   int32_t full_frequency_directivity,
+                                                   const FsgBatchTuning* tuning) {
   if (!probe || !phantoms || n_phantoms < 1 || n_phantoms > kMaxPhantoms || n_tx < 1) return 0;
   BatchPlanLayout L;
-  plan_layout(probe, phantoms, n_phantoms, n_tx, tuning, &L);
+  plan_layout(probe, phantoms, n_phantoms, n_tx, tuning, &L, full_frequency_directivity ? 1 : 0);
   return L.total;
 }
 
 static int32_t simus_batched_impl(const FsgProbe* probe, const FsgMedium* medium, const FsgPhantom* phantoms,
-                                  int32_t n_phantoms, const double* delays, const double* apod, int32_t n_tx,
+                                  int32_t n_phantoms, const double* delays, const double* apod, int32_t n_tx, int ffd,
                                   const FsgBatchTuning* tuning, const float2* tx_in, void* workspace,
                                   size_t workspace_bytes, void* stream_ptr) {
   int st = validate_batch(probe, medium, phantoms, n_phantoms, delays, n_tx);
   if (st != FSG_OK) return st;
+  if (ffd) {
+    // the per-frequency directivity is a polynomial valid for |k_f seg / 2| <= 2 pi (as in the
+    // plain sweep): sub-elements up to two wavelengths of the highest frequency wide
+    for (int p = 0; p < n_phantoms; ++p) {
+      const FsgFreqPlan& pl = phantoms[p].plan;
+      const double f_max = pl.freq_start + (pl.n_freq - 1) * pl.freq_step;
+      const double x_max = 2.0 * kPi * f_max / medium->speed_of_sound * pl.seg_length / 2.0;
+      if (x_max > 2.0 * kPi)
+        return set_error(FSG_EUNSUPPORTED,
+                         "full_frequency_directivity with sub-elements wider than two wavelengths "
+                         "(phantom %d: k_max seg / 2 = %.3f > 2 pi) is not supported by this library",
+                         p, x_max);
+    }
+  }
   BatchPlanLayout L;
-  plan_layout(probe, phantoms, n_phantoms, n_tx, tuning, &L);
+  plan_layout(probe, phantoms, n_phantoms, n_tx, tuning, &L, ffd);
   if (!workspace || workspace_bytes < L.total)
     return set_error(FSG_EWORKSPACE, "workspace of %zu bytes is smaller than the %zu bytes required", workspace_bytes,
                      L.total);
@@ -551,13 +584,14 @@ static int32_t simus_batched_impl(const FsgProbe* probe, const FsgMedium* medium
     A.tau = tau;
     A.apod = apw;
     FsgFreqPlan any = phantoms[0].plan;
-    A.C = make_sweep_const(probe, medium, &any, 0);
+    A.C = make_sweep_const(probe, medium, &any, ffd);
     convex_geometry(probe, &A.convex, &A.apex, &A.radius2);
     A.queue = queue;
     A.partial = partial;
     A.tx_in = tx_in;
     A.geo_a = reinterpret_cast<float4*>(ws + L.off_geo_a);
     A.geo_b = reinterpret_cast<float*>(ws + L.off_geo_b);
+    A.geo_c = ffd ? reinterpret_cast<float*>(ws + L.off_geo_c) : nullptr;
     if (L.max_scat > 0) {
       const int spb = E * U >= kThreads ? 1 : kThreads / (E * U);
       const int64_t want = (L.max_scat + spb - 1) / spb, cap = (int64_t)sms * 8;
@@ -588,10 +622,10 @@ static int32_t simus_batched_impl(const FsgProbe* probe, const FsgMedium* medium
 
 extern "C" int32_t fsg_simus_batched(const FsgProbe* probe, const FsgMedium* medium, const FsgPhantom* phantoms,
                                      int32_t n_phantoms, const double* delays, const double* apod, int32_t n_tx,
-                                     const FsgBatchTuning* tuning, void* workspace, size_t workspace_bytes,
-                                     void* stream) {
-  return simus_batched_impl(probe, medium, phantoms, n_phantoms, delays, apod, n_tx, tuning, nullptr, workspace,
-                            workspace_bytes, stream);
+                                     int32_t full_frequency_directivity, const FsgBatchTuning* tuning,
+                                     void* workspace, size_t workspace_bytes, void* stream) {
+  return simus_batched_impl(probe, medium, phantoms, n_phantoms, delays, apod, n_tx,
+                            full_frequency_directivity ? 1 : 0, tuning, nullptr, workspace, workspace_bytes, stream);
 }
 
 extern "C" int32_t fsg_simus_batched_rx(const FsgProbe* probe, const FsgMedium* medium, const FsgPhantom* phantom,
@@ -599,6 +633,6 @@ extern "C" int32_t fsg_simus_batched_rx(const FsgProbe* probe, const FsgMedium* 
                                         const FsgBatchTuning* tuning, void* workspace, size_t workspace_bytes,
                                         void* stream) {
   if (!tx_field) return fsg::set_error(FSG_EINVAL, "tx_field must be non-NULL");
-  return simus_batched_impl(probe, medium, phantom, 1, delays, nullptr, n_tx, tuning,
+  return simus_batched_impl(probe, medium, phantom, 1, delays, nullptr, n_tx, 0, tuning,
                             static_cast<const float2*>(tx_field), workspace, workspace_bytes, stream);
 }

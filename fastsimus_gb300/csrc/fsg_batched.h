@@ -50,6 +50,9 @@ struct BatchArgs {
   // record (geo0 + s) * E * U + e * U + u holds (r_hi, r_lo, amp, step.x) and step.y
   float4* geo_a;
   float* geo_b;
+  // full-frequency directivity: half_seg * sin(theta) per record (NULL: the centre-frequency
+  // directivity is folded into the amplitude)
+  float* geo_c;
 };
 
 struct BatchSetupArgs {

@@ -24,7 +24,7 @@
 extern "C" {
 #endif
 
-#define FSG_ABI_VERSION 2
+#define FSG_ABI_VERSION 3
 
 typedef enum FsgStatus {
   FSG_OK = 0,
@@ -155,9 +155,11 @@ typedef struct FsgBatchTuning {
   int32_t reserved0;
 } FsgBatchTuning;
 
-/* Workspace bytes needed by fsg_simus_batched. */
+/* Workspace bytes needed by fsg_simus_batched (full-frequency directivity adds one float per
+ * (scatterer, sub-element) to the geometry cache). */
 size_t fsg_simus_batched_workspace_size(const FsgProbe* probe, const FsgPhantom* phantoms, int32_t n_phantoms,
-                                        int32_t n_tx, const FsgBatchTuning* tuning);
+                                        int32_t n_tx, int32_t full_frequency_directivity,
+                                        const FsgBatchTuning* tuning);
 
 /*
  * Many transmits x many phantoms in one persistent launch.  Replaces the reference's caller
@@ -165,14 +167,16 @@ size_t fsg_simus_batched_workspace_size(const FsgProbe* probe, const FsgPhantom*
  * (tests/_picmus_phantom_shared.py:319-367, step body _simus_strategies.py:23-77): the
  * Green's terms of each (scatterer, element, frequency) are generated once and contracted with
  * every transmit.  delays/apod are device [n_tx][n_elements] float64 (apod NULL = ones; NaN
- * delay = element off).  Limits of this library: n_elements <= 128 (probes of 65-128 elements use a
+ * delay = element off).  Every probe option of fsg_simus applies (baffle, convex radius,
+ * full_frequency_directivity = simus_compute's argument of that name).  Limits of this library: n_elements <= 128 (probes of 65-128 elements use a
  * 128-element tile with one frequency per work item), n_tx <= 80, n_phantoms <= 64.
  * Phantom descriptors travel as a kernel parameter, so the call contains no host-to-device
  * copy and can be captured in a CUDA graph.
  */
 int32_t fsg_simus_batched(const FsgProbe* probe, const FsgMedium* medium, const FsgPhantom* phantoms,
                           int32_t n_phantoms, const double* delays, const double* apod, int32_t n_tx,
-                          const FsgBatchTuning* tuning, void* workspace, size_t workspace_bytes, void* stream);
+                          int32_t full_frequency_directivity, const FsgBatchTuning* tuning, void* workspace,
+                          size_t workspace_bytes, void* stream);
 
 /* Workspace bytes needed by fsg_simus_batched_tc. */
 size_t fsg_simus_batched_tc_workspace_size(const FsgProbe* probe, const FsgPhantom* phantoms, int32_t n_phantoms,

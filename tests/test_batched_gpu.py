@@ -141,3 +141,97 @@ def test_batched_phantom_without_scatterers_gives_zero():
     alone = BatchedSimus([(s, r)], delays, p, m).run()
     assert float(np.abs(np64(both[1].rf)).max()) == 0.0
     assert G.rel_l2(np64(both[0].rf), np64(alone[0].rf)) < 1e-6
+
+
+def _single_firing_goldens():
+    return [n for n in G.names("simus") if G.load(n).delays.ndim == 1]
+
+
+@pytest.mark.parametrize("name", _single_firing_goldens())
+def test_batched_matches_every_reference_golden(name):
+    """Every single-firing reference fixture through the batched sweep: soft, rigid and
+    impedance baffles, the C5-2v convex array, full-frequency directivity, three sub-elements,
+    NaN delays with apodisation, focused and plane-wave firings, 16 to 128 elements."""
+    import fastsimus_gb300 as F
+    from fastsimus_gb300.batched import BatchedSimus
+
+    g = G.load(name)
+    plan = F.simus_precompute(g.scatterers, g.rc, g.delays, g.params, g.medium, fs=g.fs,
+                              element_splitting=g.element_splitting)
+    b = BatchedSimus([(g.scatterers, g.rc)], g.delays[None], g.params, g.medium, plans=[plan],
+                     tx_apodization=g.apod, full_frequency_directivity=g.ffd)
+    rf = np64(b.run()[0].rf)[:, :, 0]
+    assert rf.shape == g.rf.shape
+    err = G.rel_l2(rf, g.rf)
+    print(f"batched {name}: relL2 {err:.3e}")
+    assert err < PLAIN_TOL
+
+
+@pytest.mark.parametrize("fb", [1, 2])
+@pytest.mark.parametrize("probe", ["c5_convex", "rigid_ffd", "impedance_split2"])
+def test_batched_probe_options_many_firings_vs_oracle(probe, fb):
+    """Probe options with several firings and two phantoms against the FP64 oracle's
+    simus_compute per firing: the C5-2v convex array with full-frequency directivity, a
+    rigid baffle with full-frequency directivity, an impedance baffle with two sub-elements.
+    fb = frequencies per work item (128-element probes always take one)."""
+    import fastsimus_gb300 as F
+    from fastsimus_gb300 import workloads as W
+    from fastsimus_gb300.batched import BatchedSimus, BatchTuning
+    from fastsimus_gb300.params import TransducerParams
+
+    m = F.MediumParams(attenuation=0.4)
+    split = None
+    if probe == "c5_convex":
+        p, ffd = G.load("simus_c5_convex").params, True
+    elif probe == "rigid_ffd":
+        p, ffd = TransducerParams(freq_center=5e6, pitch=3e-4, n_elements=40, width=2.6e-4, bandwidth=0.7,
+                                  baffle="rigid"), True
+    else:
+        p, ffd, split = TransducerParams(freq_center=4e6, pitch=3e-4, n_elements=64, width=2.5e-4, bandwidth=0.6,
+                                         baffle=1.75), False, 2
+    rng = np.random.default_rng(7)
+    top = 5e-3 if np.isinf(p.radius) else -5e-3
+    phantoms = [(W.uniform_box(rng, n, (-12e-3, 12e-3), (top, 40e-3)), rng.standard_normal(n)) for n in (130, 60)]
+    delays = W.plane_wave_delays(p, m, [-9.0, 0.0, 7.0])
+    delays[1, 3] = np.nan
+    plans = [F.simus_precompute(s, r, delays[0], p, m, element_splitting=split) for s, r in phantoms]
+    b = BatchedSimus(phantoms, delays, p, m, plans=plans, full_frequency_directivity=ffd,
+                     tuning=BatchTuning(fb, 64, 1))
+    for (s, r), plan, out in zip(phantoms, plans, b.run()):
+        rf = np64(out.rf)
+        for t in range(delays.shape[0]):
+            ref = O.simus_compute(s, r, delays[t], plan, p, m, full_frequency_directivity=ffd)
+            err = G.rel_l2(rf[:, :, t], ref.rf)
+            assert err < PLAIN_TOL, (t, err)
+
+
+def test_batched_ffd_differs_from_centre_frequency_directivity():
+    """The option is live: with full-frequency directivity the RF differs from the
+    centre-frequency directivity by more than the tolerance."""
+    from fastsimus_gb300 import workloads as W
+    from fastsimus_gb300.batched import BatchedSimus
+
+    g = G.load("simus_small_ffd")
+    delays = W.plane_wave_delays(g.params, g.medium, [0.0, 10.0])
+    a = np64(BatchedSimus([(g.scatterers, g.rc)], delays, g.params, g.medium).run()[0].rf)
+    c = np64(BatchedSimus([(g.scatterers, g.rc)], delays, g.params, g.medium,
+                          full_frequency_directivity=True).run()[0].rf)
+    assert G.rel_l2(c, a) > 100 * PLAIN_TOL
+
+
+def test_batched_ffd_wide_subelements_raise():
+    import fastsimus_gb300 as F
+    from fastsimus_gb300 import workloads as W
+    from fastsimus_gb300.batched import BatchedSimus
+    from fastsimus_gb300.params import TransducerParams
+
+    g = G.load("simus_small_ffd")
+    p = g.params
+    wide = TransducerParams(freq_center=p.freq_center, pitch=4 * p.pitch, n_elements=p.n_elements,
+                            width=3.5 * p.pitch, bandwidth=p.bandwidth)
+    d = W.plane_wave_delays(wide, g.medium, [0.0])
+    plan = F.simus_precompute(g.scatterers, g.rc, d[0], wide, g.medium, element_splitting=1)
+    with pytest.raises(NotImplementedError):
+        BatchedSimus([(g.scatterers, g.rc)], d, wide, g.medium, plans=[plan], full_frequency_directivity=True).run()
+    with pytest.raises(NotImplementedError):
+        BatchedSimus([(g.scatterers, g.rc)], d, p, g.medium, backend="tc", full_frequency_directivity=True)

@@ -124,3 +124,51 @@ def test_tc_rejects_too_many_transmits():
     s, r = W.cfg1_scatterers(100)
     with pytest.raises(NotImplementedError):
         BatchedSimus([(s, r)], W.plane_wave_delays(p, m, np.linspace(-10, 10, 97)), p, m, backend="tc").run()
+
+
+@pytest.mark.parametrize("name", ["simus_small_rigid", "simus_small_impedance", "simus_small_nan_apod",
+                                  "simus_p4_focused", "simus_cfg1_full"])
+def test_tc_matches_reference_goldens(name):
+    """Single-firing reference fixtures of up to 64 elements through the tensor-core sweep:
+    rigid and impedance baffles, NaN delays with apodisation, a focused phased-array firing."""
+    import fastsimus_gb300 as F
+    from fastsimus_gb300.batched import BatchedSimus
+
+    g = G.load(name)
+    assert not g.ffd and g.params.n_elements <= 64
+    plan = F.simus_precompute(g.scatterers, g.rc, g.delays, g.params, g.medium, fs=g.fs,
+                              element_splitting=g.element_splitting)
+    b = BatchedSimus([(g.scatterers, g.rc)], g.delays[None], g.params, g.medium, plans=[plan],
+                     tx_apodization=g.apod, backend="tc")
+    rf = np64(b.run()[0].rf)[:, :, 0]
+    assert b.device_status() == 0
+    err = G.rel_l2(rf, g.rf)
+    print(f"tc {name}: relL2 {err:.3e}")
+    assert err < TC_TOL
+
+
+@pytest.mark.parametrize("baffle", ["soft", "rigid", 1.75])
+def test_tc_convex_array_vs_oracle(baffle):
+    """A 64-element convex array (the C5-2v's pitch, width and radius) with soft, rigid and
+    impedance baffles, three firings and two phantoms, against the FP64 oracle; scatterers
+    behind the array or inside its circle contribute nothing."""
+    import dataclasses
+
+    from fastsimus_gb300 import workloads as W
+    from fastsimus_gb300.batched import BatchedSimus, BatchTuning
+
+    c5 = G.load("simus_c5_convex").params
+    p = dataclasses.replace(c5, n_elements=64, baffle=baffle)
+    m = W.cfg1_medium()
+    rng = np.random.default_rng(3)
+    phantoms = [(W.uniform_box(rng, n, (-15e-3, 15e-3), (-4e-3, 45e-3)), rng.standard_normal(n)) for n in (140, 70)]
+    delays = W.plane_wave_delays(p, m, [-10.0, 0.0, 8.0])
+    b = BatchedSimus(phantoms, delays, p, m, backend="tc", tuning=BatchTuning(5, 64, 1))
+    res = b.run()
+    assert b.device_status() == 0
+    for (s, r), plan, out in zip(phantoms, b.plans, res):
+        rf = np64(out.rf)
+        for t in range(delays.shape[0]):
+            ref = O.simus_compute(s, r, delays[t], plan, p, m)
+            err = G.rel_l2(rf[:, :, t], ref.rf)
+            assert err < TC_TOL, (t, err)
