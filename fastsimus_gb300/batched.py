@@ -92,7 +92,8 @@ class BatchedSimus:
         self.apod = None
         if tx_apodization is not None:
             a = np.broadcast_to(np.asarray(tx_apodization, dtype=np.float64), d.shape)
-            self.apod = torch.as_tensor(np.array(a, dtype=np.float64, copy=True), device=self.device)
+            self.apod = torch.as_tensor(np.array(a, dtype=np.float64, order="C", copy=True),
+                                        device=self.device).contiguous()
         self.tabs = [_device.plan_tables(p, self.device) for p in plans]
         self.outs = [torch.empty((self.n_tx, p.n_freq_full, params.n_elements), dtype=torch.complex64,
                                  device=self.device) for p in plans]

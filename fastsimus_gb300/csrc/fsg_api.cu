@@ -123,6 +123,8 @@ size_t tables_bytes(int E, int U, int F) {
   b += align256((size_t)F * 4);
   b += align256((size_t)n_anchor * E * 8);
   b += align256((size_t)E * 8);
+  b += align256((size_t)n_anchor * E * 8);
+  b += align256((size_t)E * 4);
   return b;
 }
 
@@ -138,7 +140,9 @@ Tables carve_tables(unsigned char* base, int E, int U, int F) {
   t.pp = reinterpret_cast<float2*>(base + o); o += align256((size_t)F * 8);
   t.probe = reinterpret_cast<float*>(base + o); o += align256((size_t)F * 4);
   t.da = reinterpret_cast<float2*>(base + o); o += align256((size_t)n_anchor * E * 8);
-  t.dstep = reinterpret_cast<float2*>(base + o);
+  t.dstep = reinterpret_cast<float2*>(base + o); o += align256((size_t)E * 8);
+  t.dph = reinterpret_cast<float2*>(base + o); o += align256((size_t)n_anchor * E * 8);
+  t.wtx = reinterpret_cast<float*>(base + o);
   return t;
 }
 
@@ -229,20 +233,69 @@ static int simus_grid(int n_bands, int64_t chunk_tiles, int num_sms) {
 // bounds the number of CTAs that share a band (the partial-spectrum slots per band) for any
 // chunk size: a band's ct units hold fewer than ceil(grid / n_bands) CTA starts besides its
 // first unit's CTA.
+// simus_stash_kernel shape: the fewest lanes per point (GN) whose element slots cover the probe
+// (16 source slots per lane; one, two or four per element for U = 1, 2, 3-4), with bands of
+// kTxAnchor frequencies, else of kAnchor, such that the shared memory fits.  False when no
+// shape fits (simus_band_kernel takes those probes).
+static bool stash_shape(int E, int U, int ffd, SweepConfig* c) {
+  if (U < 1 || U > 4) return false;
+  const int spe = U == 1 ? 1 : (U == 2 ? 2 : 4);
+  const int epl = kSrcPerThread / spe;
+  // the warp-specialised kernel: E = 64, 128 (any U) or 256 (U <= 2); 128 transmit threads
+  if ((E == 64 || E == 128 || (E == 256 && U <= 2))) {
+    int gn = E * spe / kSrcPerThread;
+    if (gn < 4) gn = 4;
+    const int st = 128 / gn, fb = E > 128 ? 32 : 64;
+    const int pad = choose_plane_pad(E, U, gn, st);
+    const WsLayout L = ws_layout(st, fb, E, U, pad, ffd != 0);
+    if (gn <= 32 && L.total <= kMaxDynSmem - 1024) {
+      c->kind = 2;
+      c->gn = gn;
+      c->st = st;
+      c->fb = fb;
+      c->plane_pad = pad;
+      c->smem = L.total;
+      c->geo_bytes = L.g.geo_bytes;
+      return true;
+    }
+  }
+  for (int fb = kTxAnchor; fb >= kAnchor; fb /= 2) {
+    for (int gn = 4; gn <= 32; gn *= 2) {
+      if (gn * epl < E) continue;
+      const int st = kThreads / gn;
+      const int pad = choose_plane_pad(E, U, gn, st);
+      const StashLayout L = stash_layout(st, fb, E, U, pad, ffd != 0);
+      if (L.total > kMaxDynSmem - 1024) continue;
+      c->kind = 1;
+      c->gn = gn;
+      c->st = st;
+      c->fb = fb;
+      c->plane_pad = pad;
+      c->smem = L.total;
+      c->geo_bytes = L.g.geo_bytes;
+      return true;
+    }
+  }
+  return false;
+}
+
 SweepConfig simus_config(int E, int U, int F, int64_t n_scat, int num_sms, size_t cache_budget, int ffd) {
   SweepConfig c;
-  const int n_src = E * U;
-  c.gn = next_pow2((n_src + kSrcPerThread - 1) / kSrcPerThread);
-  if (c.gn < 4) c.gn = 4;
-  c.st = kThreads / c.gn;
-  int runs = kThreads / E;
-  if (runs > 4) runs = 4;
-  c.fb = kAnchor * runs;
+  if (!stash_shape(E, U, ffd, &c)) {
+    const int n_src = E * U;
+    c.kind = 0;
+    c.gn = next_pow2((n_src + kSrcPerThread - 1) / kSrcPerThread);
+    if (c.gn < 4) c.gn = 4;
+    c.st = kThreads / c.gn;
+    int runs = kThreads / E;
+    if (runs > 4) runs = 4;
+    c.fb = kAnchor * runs;
+    c.plane_pad = choose_plane_pad(E, U, c.gn, c.st);
+    const SmemLayout L = smem_layout(c.st, c.fb, E, U, c.plane_pad, true, ffd != 0);
+    c.smem = L.total;
+    c.geo_bytes = L.geo_bytes;
+  }
   c.n_bands = (F + c.fb - 1) / c.fb;
-  c.plane_pad = choose_plane_pad(E, U, c.gn, c.st);
-  const SmemLayout L = smem_layout(c.st, c.fb, E, U, c.plane_pad, true, ffd != 0);
-  c.smem = L.total;
-  c.geo_bytes = L.geo_bytes;
   c.per_slice = 0;
   const int64_t tiles = n_scat > 0 ? (n_scat + c.st - 1) / c.st : 1;
   int64_t ct = (int64_t)(cache_budget / c.geo_bytes);
@@ -256,6 +309,7 @@ SweepConfig simus_config(int E, int U, int F, int64_t n_scat, int num_sms, size_
 
 SweepConfig pfield_config(int E, int U, int F, int64_t n_pts, int num_sms, int ffd) {
   SweepConfig c;
+  c.kind = 0;
   const int n_src = E * U;
   c.gn = next_pow2((n_src + kSrcPerThread - 1) / kSrcPerThread);
   if (c.gn < 4) c.gn = 4;
@@ -411,10 +465,10 @@ extern "C" int32_t fsg_simus(const FsgProbe* probe, const FsgMedium* medium, con
   const int full = out_layout == FSG_OUT_FULL_CORRECTED;
   const int rows = full ? plan->n_freq_full : F;
   const int64_t n_out = (int64_t)rows * E;
-  simus_reduce<<<(unsigned)((n_out + 255) / 256), 256, 0, s>>>(partial, n_scat > 0 ? c.n_slices : 0, F, E, t.probe,
-                                                               full ? (float)plan->correction_factor : 1.0f, full,
-                                                               rows, plan->freq_idx_start, status,
-                                                               static_cast<float2*>(out));
+  simus_reduce<<<(unsigned)((n_out + 255) / 256), 256, 0, s>>>(
+      partial, n_scat > 0 ? c.n_slices : 0, F, E, t.probe, full ? (float)plan->correction_factor : 1.0f, full, rows,
+      plan->freq_idx_start, status, c.kind >= 1 ? delays : nullptr, plan->freq_start, plan->freq_step,
+      static_cast<float2*>(out));
   return check_cuda(cudaGetLastError(), "simus_reduce launch");
 }
 

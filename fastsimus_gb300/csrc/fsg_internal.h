@@ -19,6 +19,8 @@ struct Tables {
   float* probe;      // [F]
   float2* da;        // [n_anchor][E] apod * exp(i 2 pi f_anchor tau)
   float2* dstep;     // [E] exp(i 2 pi df tau)
+  float2* dph;       // [n_anchor][E] exp(i 2 pi f_anchor tau) (no apodization; NULL: not written)
+  float* wtx;        // [E] transmit apodization, 0 for an element whose delay is NaN
 };
 
 struct SetupArgs {
@@ -102,7 +104,57 @@ __host__ __device__ inline SmemLayout smem_layout(int st, int fb, int E, int U, 
   return L;
 }
 
+// simus_stash_kernel: frequencies per stash sub-block, and its shared memory.  Region 0 holds
+// first the tile's geometry block (SmemLayout offsets) and then the stash [st][kStashFreqs][ep]
+// of complex Green's terms, ep = E rounded up to odd (the transmit lanes of 2 to 8 points write
+// one sub-block row each without bank conflicts).
+constexpr int kStashFreqs = 8;
+constexpr size_t kMaxDynSmem = 227 * 1024;
+struct StashLayout {
+  SmemLayout g;
+  int ep;
+  size_t off_w, off_pp, off_kb, off_dph, off_dstep, off_y, total;
+};
+__host__ __device__ inline StashLayout stash_layout(int st, int fb, int E, int U, int plane_pad, bool ffd) {
+  StashLayout S;
+  S.g = smem_layout(st, fb, E, U, plane_pad, true, ffd);
+  S.ep = E | 1;
+  const size_t stash = (size_t)st * kStashFreqs * S.ep * 8;
+  size_t o = align16(S.g.geo_bytes > stash ? S.g.geo_bytes : stash);
+  S.off_w = o; o = align16(o + (size_t)st * kStashFreqs * 8);
+  S.off_pp = o; o = align16(o + (size_t)fb * 8);
+  S.off_kb = o; o = align16(o + (ffd ? (size_t)fb * 4 : 0));
+  S.off_dph = o; o = align16(o + (size_t)E * 8);
+  S.off_dstep = o; o = align16(o + (size_t)E * 8);
+  S.off_y = o; o = align16(o + (size_t)fb * E * 8);
+  S.total = o;
+  return S;
+}
+
+// simus_ws_kernel: the tile's geometry block from offset 0, then two stash buffers
+// [stx][kStashFreqs][ep], two W buffers [stx][kStashFreqs] and the band tables.
+struct WsLayout {
+  SmemLayout g;  // the tile's geometry block, from offset 0
+  int ep;
+  size_t off_stash, off_w, off_pp, off_kb, off_dph, off_dstep, total;
+};
+__host__ __device__ inline WsLayout ws_layout(int stx, int fb, int E, int U, int plane_pad, bool ffd) {
+  WsLayout S;
+  S.g = smem_layout(stx, fb, E, U, plane_pad, true, ffd);
+  S.ep = E | 1;
+  size_t o = (S.g.geo_bytes + 127) & ~size_t(127);
+  S.off_stash = o; o = align16(o + 2 * (size_t)stx * kStashFreqs * S.ep * 8);
+  S.off_w = o; o = align16(o + 2 * (size_t)stx * kStashFreqs * 8);
+  S.off_pp = o; o = align16(o + (size_t)fb * 8);
+  S.off_kb = o; o = align16(o + (ffd ? (size_t)fb * 4 : 0));
+  S.off_dph = o; o = align16(o + (size_t)E * 8);
+  S.off_dstep = o; o = align16(o + (size_t)E * 8);
+  S.total = o;
+  return S;
+}
+
 struct SweepConfig {
+  int kind;            // simus: 0 = simus_band_kernel, 1 = simus_stash_kernel
   int gn, st, fb, n_bands, plane_pad;
   int n_slices;        // pfield: point slices; simus: partial-spectrum slots per band
   int64_t per_slice;   // pfield: points per slice
@@ -115,13 +167,19 @@ struct SweepConfig {
 __global__ void setup_tables(SetupArgs a);
 // Geometry of every (scatterer, source) of one chunk into A.geo (tile-major SmemLayout blocks).
 __global__ void geometry_kernel(const BandArgs A, int64_t chunk_tiles);
-// Launches simus_band_kernel<U> (U = n_sub in 1..4) with c's grid and shared memory.
+// Launches simus_band_kernel<U> or simus_stash_kernel<U> (U = n_sub in 1..4), as c.kind says,
+// with c's grid and shared memory.
 cudaError_t launch_simus_band_any(int U, const SweepConfig& c, const BandArgs& A, cudaStream_t s);
+cudaError_t launch_simus_stash(int U, const SweepConfig& c, const BandArgs& A, cudaStream_t s);
+cudaError_t launch_simus_stash_ffd(int U, const SweepConfig& c, const BandArgs& A, cudaStream_t s);
 // Launches pfield_band_kernel<gn> with c's grid and shared memory.
 cudaError_t launch_pfield_band_any(const SweepConfig& c, const BandArgs& A, cudaStream_t s);
+// rx_delays (NULL: none) undoes the transmit delay phase that the stash kernel leaves on its
+// receive sums: out *= exp(-i 2 pi (f0 + f df) tau_e), tau_e = rx_delays[e] (NaN = 0).
 __global__ void simus_reduce(const float2* __restrict__ partial, int n_slices, int F, int E,
                              const float* __restrict__ probe, float corr, int full, int n_rows, int idx0,
-                             const int* __restrict__ status, float2* __restrict__ out);
+                             const int* __restrict__ status, const double* __restrict__ rx_delays, double f0,
+                             double df, float2* __restrict__ out);
 __global__ void pfield_reduce(const float* __restrict__ partial, int n_bands, int64_t n_pts, float corr,
                               float* __restrict__ out);
 

@@ -79,7 +79,9 @@ __global__ void setup_tables(SetupArgs a) {
     double s, c;
     sincos(2.0 * kPi * f * tau, &s, &c);
     a.t.da[i] = make_float2((float)(w * c), (float)(w * s));
+    if (a.t.dph) a.t.dph[i] = make_float2((float)c, (float)s);
     if (m == 0) {
+      if (a.t.wtx) a.t.wtx[e] = (float)w;
       sincos(2.0 * kPi * a.df * tau, &s, &c);
       a.t.dstep[e] = make_float2((float)c, (float)s);
     }
@@ -122,7 +124,8 @@ __global__ void __launch_bounds__(kThreads) geometry_kernel(const BandArgs A, in
 // out (layout) = probe_f * corr * sum over slots of partial[q][f][e], fixed slot order.
 __global__ void simus_reduce(const float2* __restrict__ partial, int n_slices, int F, int E,
                              const float* __restrict__ probe, float corr, int full, int n_rows, int idx0,
-                             const int* __restrict__ status, float2* __restrict__ out) {
+                             const int* __restrict__ status, const double* __restrict__ rx_delays, double f0,
+                             double df, float2* __restrict__ out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (int64_t)n_rows * E) return;
   if (*status != FSG_OK) {  // a sweep CTA gave up waiting: make the failure visible in the output
@@ -136,6 +139,13 @@ __global__ void simus_reduce(const float2* __restrict__ partial, int n_slices, i
     for (int q = 0; q < n_slices; ++q) acc = cadd(acc, partial[((size_t)q * F + f) * E + e]);
     float s = probe[f] * corr;
     acc = make_float2(acc.x * s, acc.y * s);
+    if (rx_delays) {
+      double tau = rx_delays[e];
+      if (isnan(tau)) tau = 0.0;
+      double sn, cs;
+      sincos(2.0 * kPi * (f0 + f * df) * tau, &sn, &cs);
+      acc = cmul(acc, make_float2((float)cs, (float)-sn));
+    }
   }
   out[i] = acc;
 }
@@ -150,6 +160,7 @@ __global__ void pfield_reduce(const float* __restrict__ partial, int n_bands, in
 }
 
 cudaError_t launch_simus_band_any(int U, const SweepConfig& c, const BandArgs& A, cudaStream_t s) {
+  if (c.kind >= 1) return A.C.ffd ? launch_simus_stash_ffd(U, c, A, s) : launch_simus_stash(U, c, A, s);
   return A.C.ffd ? launch_simus_band_ffd(U, c, A, s) : launch_simus_band_u<false>(U, c, A, s);
 }
 

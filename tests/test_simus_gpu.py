@@ -224,3 +224,33 @@ def test_full_frame_plan_matches_reference_golden():
     err_c = G.rel_l2(chunked, g.spectrum_selected)
     print(f"full plan, 512-scatterer workspace (chunked): spectrum relL2 {err_c:.3e}")
     assert err_c < PLAIN_TOL
+
+
+@pytest.mark.parametrize("n_elements,splitting,ffd,baffle", [
+    (256, 1, False, "soft"), (256, 2, True, "rigid"), (128, 1, False, 1.5), (128, 3, False, "soft"),
+    (128, 4, True, "soft"), (64, 4, False, "rigid"), (64, 1, True, "soft"),
+    (192, 2, False, "soft"), (48, 2, True, 1.5), (160, 3, False, "soft")])
+def test_sweep_kernel_shapes_vs_oracle(n_elements, splitting, ffd, baffle):
+    """Every sweep kernel against the FP64 oracle: the warp-specialised stash kernel (64, 128
+    and 256 elements, one to four sub-elements, with and without full-frequency directivity),
+    the single-role stash kernel (192 and 48 elements) and the re-generating band kernel (160
+    elements x 3 sub-elements, whose 16-slot lanes the stash kernels cannot map)."""
+    import fastsimus_gb300 as F
+    from fastsimus_gb300.params import TransducerParams
+
+    p = TransducerParams(freq_center=4e6, pitch=3e-4, n_elements=n_elements, width=2.7e-4, bandwidth=0.6,
+                         baffle=baffle)
+    m = F.MediumParams(attenuation=0.4)
+    rng = np.random.default_rng(n_elements + splitting)
+    n = 140
+    s = np.stack([rng.uniform(-15e-3, 15e-3, n), rng.uniform(3e-3, 35e-3, n)], axis=-1)
+    r = rng.standard_normal(n)
+    d = np.linspace(0.0, 2e-6, n_elements)
+    d[3] = np.nan
+    apod = np.hanning(n_elements) + 0.1
+    plan = F.simus_precompute(s, r, d, p, m, element_splitting=splitting)
+    got = np64(F.simus_compute(s, r, d, plan, p, m, tx_apodization=apod, full_frequency_directivity=ffd).rf)
+    ref = O.simus_compute(s, r, d, plan, p, m, tx_apodization=apod, full_frequency_directivity=ffd)
+    err = G.rel_l2(got, ref.rf)
+    print(f"E={n_elements} U={splitting} ffd={ffd} baffle={baffle}: relL2 {err:.2e}")
+    assert err < PLAIN_TOL
