@@ -45,11 +45,11 @@ WORKLOAD = ("cfg2: 128-element linear array (pitch 0.30 mm, width 0.27 mm, fc 5.
             "c 1540 m/s, 0.5 dB/cm/MHz, 0-degree plane wave, 200,000 scatterers x in [-19,19] mm, "
             "z in [5,50] mm, rc N(0,1) with three 2 mm anechoic disks; + pfield on 256x512 grid")
 L2_FLUSH_BYTES = 512 << 20
-# DRAM bytes (read + write) of one simus_band_kernel launch measured by ncu on an 8,816-scatterer
+# DRAM bytes (read + write) of one simus_ws_kernel launch measured by ncu on an 8,720-scatterer
 # chunk, the chunk size of the benchmark frame: the tile geometry blocks read once from HBM
 # (then from L2 by the other bands' CTAs) plus the partial spectra.  The bench cannot run ncu;
 # the figure is refreshed from a capture whenever the kernel changes.
-BAND_KERNEL_DRAM_BYTES = 61_555_456 + 1_743_616
+BAND_KERNEL_DRAM_BYTES = 61_484_032 + 1_643_776
 
 
 def _env_int(name, default):
@@ -454,11 +454,11 @@ def run_gpu_arm(args, rank, world):
         "green_terms_per_s": gt * value,
         "simus_ms": simus_avg, "pfield_ms": float(np.mean(pfield_ms)) if pfield_ms else None,
         "gpu_launches": args.steps * frame_launches(plan, params, n_scat, device),
-        "roofline": {"kernel": "simus_band_kernel", "bound": "fp32", "achieved": achieved, "peak": peak,
+        "roofline": {"kernel": "simus_ws_kernel", "bound": "fp32", "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                     "traffic": BAND_KERNEL_DRAM_BYTES, "traffic_unit": "bytes per band-kernel launch",
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one simus_band_kernel "
-                                       "launch on an 8,816-scatterer chunk (the chunk size of this frame), "
+                     "traffic": BAND_KERNEL_DRAM_BYTES, "traffic_unit": "bytes per sweep-kernel launch",
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one simus_ws_kernel "
+                                       "launch on an 8,720-scatterer chunk (the chunk size of this frame), "
                                        "python bench.py --steps 1 --warmup 1 --no-e2e --scatterers 20000",
                      "peak_source": "measured in-run by fsg_fp32_fma_probe (FP32 FMA chains); MEASURED_PEAKS.json "
                                     "holds only HBM and bf16 tensor peaks",
