@@ -738,12 +738,18 @@ def run_batched_workload(args):
     b = BatchedSimus(phantoms, delays, p, m)
     t_plan = time.perf_counter() - t0
     t0 = time.perf_counter()
-    from fastsimus_gb300.batched import BatchTuning
+    from fastsimus_gb300.batched import BatchTuning, fp32_search_space
 
-    # the quick list holds the shapes the full autotune settles on for this workload
-    quick = ([BatchTuning(2, 8192, 1), BatchTuning(1, 8192, 1), BatchTuning(2, 32768, 1)]
-             if getattr(args, "autotune_quick", False) else None)
-    best = b.autotune(candidates=quick, cache=False)
+    # tile-shape search: every compiled FP32 shape x two chunk sizes for this batch, timed on a
+    # slice of the batch (its first phantoms: same probe, firings and per-item shapes); the
+    # winner runs the full batch
+    space = fp32_search_space(p.n_elements, sum(int(s.shape[0]) for s, _ in b.phantoms))
+    n_slice = min(len(phantoms), 3)
+    tuner = BatchedSimus(phantoms[:n_slice], delays, p, m, plans=b.plans[:n_slice])
+    best = tuner.autotune(candidates=space, cache=False)
+    tune_log = sorted(({"ms": round(t, 3), **c} for t, c in tuner.tune_log), key=lambda r: r["ms"])
+    del tuner
+    b.set_tuning(best)
     t_tune = time.perf_counter() - t0
     b.capture()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
@@ -788,7 +794,9 @@ def run_batched_workload(args):
             "roofline": {"kernel": "batched_kernel", "bound": "fp32", "achieved": flops / (sweep_ms * 1e-3) / 1e12,
                          "peak": peak, "unit": "TFLOP/s", "frac": flops / (sweep_ms * 1e-3) / 1e12 / peak,
                          "algorithmic_flops_per_launch": flops},
-            "autotune_log": getattr(b, "tune_log", None), "clocks": clocks.summary()}
+            "autotune": {"searched_on": f"the first {n_slice} phantoms of the batch, one sweep per candidate",
+                         "space": [c.__dict__ for c in space], "log_ms": tune_log, "winner": best.__dict__},
+            "clocks": clocks.summary()}
     # the same batch on the tensor cores (BF16 hi/lo, 1e-3 accuracy class), checked against the
     # FP32 spectra above
     try:

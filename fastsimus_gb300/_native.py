@@ -17,7 +17,7 @@ LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libfsgb300.so"
 FSG_OK, FSG_EINVAL, FSG_ECUDA, FSG_ETIMEOUT, FSG_EUNSUPPORTED, FSG_EWORKSPACE = range(6)
 FSG_BAFFLE_SOFT, FSG_BAFFLE_RIGID, FSG_BAFFLE_IMPEDANCE = range(3)
 FSG_OUT_SELECTED_RAW, FSG_OUT_FULL_CORRECTED = range(2)
-ABI_VERSION = 3
+ABI_VERSION = 4
 
 
 class FsgError(RuntimeError):
@@ -83,7 +83,8 @@ class FsgMlpTrain(ctypes.Structure):
 
 class FsgBatchTuning(ctypes.Structure):
     _fields_ = [("freqs_per_item", ctypes.c_int32), ("chunk_scatterers", ctypes.c_int32),
-                ("ctas_per_sm", ctypes.c_int32), ("reserved0", ctypes.c_int32)]
+                ("ctas_per_sm", ctypes.c_int32), ("tile_scatterers", ctypes.c_int32), ("packed", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 3)]
 
 
 FSG_DAS_LINEAR, FSG_DAS_NEAREST = range(2)

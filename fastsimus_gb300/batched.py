@@ -34,18 +34,38 @@ _DEFAULT_MEDIUM = MediumParams()
 @dataclass(frozen=True)
 class BatchTuning:
     """Tile shapes of the batched sweep: frequencies per work item (1 or 2; probes of more
-    than 64 elements always use 1), scatterers per work item, persistent CTAs per SM."""
+    than 64 elements always use 1), scatterers per work item, persistent CTAs per SM, and for
+    the FP32 kernel the scatterers per tile (32, 64, 128) and the FP32x2-packed register tile.
+    ``FP32_SHAPES`` lists the compiled (freqs_per_item, elements tile, tile_scatterers,
+    packed, ctas_per_sm) combinations."""
 
     freqs_per_item: int = 2
     chunk_scatterers: int = 32768
     ctas_per_sm: int = 1
+    tile_scatterers: int = 64
+    packed: int = 0
 
     @staticmethod
     def default(backend: str) -> "BatchTuning":
         return BatchTuning(7, 16384, 1) if backend == "tc" else BatchTuning()
 
     def to_c(self) -> _native.FsgBatchTuning:
-        return _native.FsgBatchTuning(self.freqs_per_item, self.chunk_scatterers, self.ctas_per_sm, 0)
+        return _native.FsgBatchTuning(self.freqs_per_item, self.chunk_scatterers, self.ctas_per_sm,
+                                      self.tile_scatterers, self.packed)
+
+
+# (freqs_per_item, elements tile, tile_scatterers, packed, ctas_per_sm) compiled into batched_kernel
+FP32_SHAPES = ((2, 64, 64, 0, 1), (2, 64, 32, 0, 1), (1, 64, 64, 0, 1), (1, 64, 32, 0, 1), (1, 64, 128, 0, 1),
+               (1, 64, 64, 1, 1), (1, 64, 32, 1, 1), (1, 64, 32, 0, 2), (1, 128, 64, 0, 1), (1, 128, 32, 0, 1))
+
+
+def fp32_search_space(n_elements: int, total_scatterers: int) -> list[BatchTuning]:
+    """The FP32 autotuner's candidates: every compiled tile shape for the probe's element tile,
+    each with two chunk sizes bracketing the batch (items enough to fill the SMs)."""
+    eb = 64 if n_elements <= 64 else 128
+    chunks = sorted({c for c in (8192, 16384, 32768, 65536) if c < 2 * max(total_scatterers, 64)} or {8192})
+    chunks = [chunks[0], chunks[-1]] if len(chunks) > 1 else chunks
+    return [BatchTuning(fb, c, cps, bt, pk) for fb, e, bt, pk, cps in FP32_SHAPES if e == eb for c in chunks]
 
 
 def shared_plan(scatterers, rc, delays_list, params: TransducerParams, medium: MediumParams, **plan_kw) -> SimusPlan:
@@ -228,10 +248,7 @@ class BatchedSimus:
             candidates = [BatchTuning(fb, c, 1) for fb in range(max(1, top - 2), top + 1) for c in (8192, 16384)]
         if candidates is None:
             total = sum(int(s.shape[0]) for s, _ in self.phantoms)
-            chunks = sorted({c for c in (8192, 16384, 32768, 65536, 131072) if c < 2 * max(total, 64)} or {8192})
-            # probes of more than 64 elements use the 128-element tile, one frequency per item
-            fbs = (1,) if self.params.n_elements > 64 else (1, 2)
-            candidates = [BatchTuning(fb, c, 1) for fb in fbs for c in chunks[:: max(1, len(chunks) // 2)]]
+            candidates = fp32_search_space(self.params.n_elements, total)
         timings = []
         for cand in candidates:
             self.set_tuning(cand)

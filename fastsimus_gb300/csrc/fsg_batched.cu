@@ -24,6 +24,8 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <type_traits>
+
 #include "../../include/fsgb300.h"
 #include "fsg_batched.h"
 #include "fsg_common.cuh"
@@ -31,7 +33,6 @@
 
 namespace fsg {
 
-constexpr int kBT = 64;        // scatterers per tile
 constexpr int kBTX = 80;       // padded transmits
 constexpr int kWPitch = 81;    // complex per W / D row
 // Elements are padded to EB = 64 or 128 (a template parameter); a Gm row holds EB + 1 complex
@@ -58,16 +59,30 @@ __device__ __forceinline__ float2 cis_two_pi_ftau(float2 f, float2 tau) {
   return make_float2(c, s);
 }
 
-// EB padded elements: the receive register tile is EB/16 element rows x 5 transmits per thread.
-template <int FB, int EB>
-__global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_constant__ BatchArgs A) {
+// The B operands (D of the transmit product, W of the receive product) of the packed register
+// tile: (b.x, b.y, -b.y, b.x), so that acc + a b is two FP32x2 FMAs with a broadcast,
+// (acc.x, acc.y) + (a.x, a.x)(b.x, b.y) + (a.y, a.y)(-b.y, b.x), rounding exactly like cfma.
+__device__ __forceinline__ float4 pk_operand(float2 b) { return make_float4(b.x, b.y, -b.y, b.x); }
+__device__ __forceinline__ float2 pk_cfma(float2 a, float4 b, float2 acc) {
+  acc = __ffma2_rn(make_float2(a.x, a.x), make_float2(b.x, b.y), acc);
+  return __ffma2_rn(make_float2(a.y, a.y), make_float2(b.z, b.w), acc);
+}
+
+// FB frequencies per item, EB padded elements, BT scatterers per tile; the transmit register
+// tile is BT/16 scatterer rows x 5 transmits per thread, the receive tile EB/16 element rows x
+// 5 transmits.  PK: the complex MACs on the FP32x2 pipe with (b, conj-swapped b) operands in
+// shared memory.  MINB: CTAs per SM the register budget is cut for.
+template <int FB, int EB, int BT, bool PK, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) batched_kernel(const __grid_constant__ BatchArgs A) {
   extern __shared__ __align__(16) unsigned char sm[];
   constexpr int kGmPitch = gm_pitch(EB);
   constexpr int kRows = EB / 16;                                     // receive rows per thread
-  float2* Gm = reinterpret_cast<float2*>(sm);                       // [FB][kBT][kGmPitch]
-  float2* D = Gm + FB * kBT * kGmPitch;                              // [FB][EB][kWPitch]
-  float2* W = D + FB * EB * kWPitch;                                 // [kBT][kWPitch]
-  float* rcs = reinterpret_cast<float*>(W + kBT * kWPitch);          // [kBT]
+  constexpr int kTRows = BT / 16;                                    // transmit rows per thread
+  using BOp = typename std::conditional<PK, float4, float2>::type;  // a B-operand entry
+  float2* Gm = reinterpret_cast<float2*>(sm);                       // [FB][BT][kGmPitch]
+  BOp* D = reinterpret_cast<BOp*>(Gm + FB * BT * kGmPitch);          // [FB][EB][kWPitch]
+  BOp* W = D + FB * EB * kWPitch;                                    // [BT][kWPitch]
+  float* rcs = reinterpret_cast<float*>(W + BT * kWPitch);           // [BT]
   __shared__ int s_item;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -105,7 +120,8 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
           v = make_float2(w * c.x, w * c.y);
         }
       }
-      D[(f * EB + e) * kWPitch + t] = v;
+      if constexpr (PK) D[(f * EB + e) * kWPitch + t] = pk_operand(v);
+      else D[(f * EB + e) * kWPitch + t] = v;
     }
     // band constants
     float2 pp[FB];
@@ -126,9 +142,9 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
 #pragma unroll
         for (int j = 0; j < 5; ++j) Y[f][i][j] = make_float2(0.f, 0.f);
 
-    for (int64_t t0 = s_begin; t0 < s_end; t0 += kBT) {
+    for (int64_t t0 = s_begin; t0 < s_end; t0 += BT) {
       // --- the tile's reflectivities (0 out of field) ---
-      if (tid < kBT) {
+      if (tid < BT) {
         const int64_t s = t0 + tid;
         float w = 0.f;
         if (s < s_end) {
@@ -140,9 +156,9 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
         rcs[tid] = w;
       }
       __syncthreads();
-      // --- Green's matrix Gm[f][s][e] for the tile: thread (e, s-group of kBT * EB / 256) ---
+      // --- Green's matrix Gm[f][s][e] for the tile: thread (e, s-group of BT * EB / 256) ---
       {
-        constexpr int kSpg = kBT * EB / kThreads;
+        constexpr int kSpg = BT * EB / kThreads;
         const int e = tid % EB;
         const int sg = tid / EB;
         for (int k = 0; k < kSpg; ++k) {
@@ -171,16 +187,16 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
             }
           }
           Gm[sl * kGmPitch + e] = g0;
-          if (FB > 1) Gm[(kBT + sl) * kGmPitch + e] = g1;
+          if (FB > 1) Gm[(BT + sl) * kGmPitch + e] = g1;
         }
       }
       __syncthreads();
 #pragma unroll
       for (int f = 0; f < FB; ++f) {
-        const float2* G = Gm + f * kBT * kGmPitch;
+        const float2* G = Gm + f * BT * kGmPitch;
         if (A.tx_in) {
           // transmit field supplied by the caller (already includes pulse * probe): W = rc * p
-          for (int i = tid; i < kBT * kBTX; i += kThreads) {
+          for (int i = tid; i < BT * kBTX; i += kThreads) {
             const int sl = i / kBTX, t = i % kBTX;
             const int64_t sg = t0 + sl;
             float2 v = make_float2(0.f, 0.f);
@@ -188,43 +204,54 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
               const float2 pv = A.tx_in[((size_t)sg * P.n_freq + (f0 + f)) * T + t];
               v = make_float2(rcs[sl] * pv.x, rcs[sl] * pv.y);
             }
-            W[sl * kWPitch + t] = v;
+            if constexpr (PK) W[sl * kWPitch + t] = pk_operand(v);
+            else W[sl * kWPitch + t] = v;
           }
         } else {
-          // --- TX: P[s][t] = sum_e G[s][e] D[e][t]; thread rows s = wm*16 + lm + 4i, cols t = wn*40 + ln*5 + j
-          float2 acc[4][5];
+          // --- TX: P[s][t] = sum_e G[s][e] D[e][t]; thread rows s = wm*(BT/4) + lm + 4i,
+          //     cols t = wn*40 + ln*5 + j
+          float2 acc[kTRows][5];
   #pragma unroll
-          for (int i = 0; i < 4; ++i)
+          for (int i = 0; i < kTRows; ++i)
   #pragma unroll
             for (int j = 0; j < 5; ++j) acc[i][j] = make_float2(0.f, 0.f);
-          const float2* Df = D + f * EB * kWPitch;
+          const BOp* Df = D + f * EB * kWPitch;
   #pragma unroll 4
           for (int e = 0; e < EB; ++e) {
-            float2 a[4], b[5];
+            float2 a[kTRows];
+            BOp b[5];
   #pragma unroll
-            for (int i = 0; i < 4; ++i) a[i] = G[(wm * 16 + lm + 4 * i) * kGmPitch + e];
+            for (int i = 0; i < kTRows; ++i) a[i] = G[(wm * (BT / 4) + lm + 4 * i) * kGmPitch + e];
   #pragma unroll
             for (int j = 0; j < 5; ++j) b[j] = Df[e * kWPitch + wn * 40 + ln * 5 + j];
   #pragma unroll
-            for (int i = 0; i < 4; ++i)
+            for (int i = 0; i < kTRows; ++i)
   #pragma unroll
-              for (int j = 0; j < 5; ++j) acc[i][j] = cfma(a[i], b[j], acc[i][j]);
+              for (int j = 0; j < 5; ++j) {
+                if constexpr (PK) acc[i][j] = pk_cfma(a[i], b[j], acc[i][j]);
+                else acc[i][j] = cfma(a[i], b[j], acc[i][j]);
+              }
           }
           // W[s][t] = rc_s * pulse * probe * P
   #pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            const int s = wm * 16 + lm + 4 * i;
+          for (int i = 0; i < kTRows; ++i) {
+            const int s = wm * (BT / 4) + lm + 4 * i;
             const float w = rcs[s];
             const float2 sc = make_float2(w * pp[f].x, w * pp[f].y);
   #pragma unroll
-            for (int j = 0; j < 5; ++j) W[s * kWPitch + wn * 40 + ln * 5 + j] = cmul(sc, acc[i][j]);
+            for (int j = 0; j < 5; ++j) {
+              const float2 v = cmul(sc, acc[i][j]);
+              if constexpr (PK) W[s * kWPitch + wn * 40 + ln * 5 + j] = pk_operand(v);
+              else W[s * kWPitch + wn * 40 + ln * 5 + j] = v;
+            }
           }
         }
         __syncthreads();
         // --- RX: Y[e][t] += sum_s G[s][e] W[s][t]; thread rows e = wm*(EB/4) + lm + 4i
 #pragma unroll 4
-        for (int s = 0; s < kBT; ++s) {
-          float2 a[kRows], b[5];
+        for (int s = 0; s < BT; ++s) {
+          float2 a[kRows];
+          BOp b[5];
 #pragma unroll
           for (int i = 0; i < kRows; ++i) a[i] = G[s * kGmPitch + wm * (EB / 4) + lm + 4 * i];
 #pragma unroll
@@ -232,7 +259,10 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(const __grid_const
 #pragma unroll
           for (int i = 0; i < kRows; ++i)
 #pragma unroll
-            for (int j = 0; j < 5; ++j) Y[f][i][j] = cfma(a[i], b[j], Y[f][i][j]);
+            for (int j = 0; j < 5; ++j) {
+              if constexpr (PK) Y[f][i][j] = pk_cfma(a[i], b[j], Y[f][i][j]);
+              else Y[f][i][j] = cfma(a[i], b[j], Y[f][i][j]);
+            }
         }
         __syncthreads();
       }
@@ -339,24 +369,44 @@ __global__ void __launch_bounds__(kThreads) batched_geometry_kernel(const __grid
   }
 }
 
-size_t batched_smem_bytes(int fb, int eb) {
-  return (size_t)(fb * kBT * gm_pitch(eb) + fb * eb * kWPitch + kBT * kWPitch) * sizeof(float2) + kBT * sizeof(float);
+size_t batched_smem_bytes(int fb, int eb, int bt, int pk) {
+  const size_t bop = pk ? sizeof(float4) : sizeof(float2);
+  return (size_t)fb * bt * gm_pitch(eb) * sizeof(float2) + ((size_t)fb * eb * kWPitch + (size_t)bt * kWPitch) * bop +
+         bt * sizeof(float);
 }
 
 int batched_pad_elements(int n_elements) { return n_elements <= 64 ? 64 : 128; }
 
-template <int FB, int EB>
+template <int FB, int EB, int BT, bool PK, int MINB>
 static cudaError_t launch_batched_t(int grid, const BatchArgs& A, cudaStream_t s) {
-  const size_t smem = batched_smem_bytes(FB, EB);
-  cudaError_t e = cudaFuncSetAttribute(batched_kernel<FB, EB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const size_t smem = batched_smem_bytes(FB, EB, BT, PK);
+  auto k = batched_kernel<FB, EB, BT, PK, MINB>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  batched_kernel<FB, EB><<<grid, kThreads, smem, s>>>(A);
+  k<<<grid, kThreads, smem, s>>>(A);
   return cudaGetLastError();
 }
 
-cudaError_t launch_batched(int fb, int eb, int grid, const BatchArgs& A, cudaStream_t s) {
-  if (eb == 128) return launch_batched_t<1, 128>(grid, A, s);  // the 128-element tile fits one frequency
-  return fb == 1 ? launch_batched_t<1, 64>(grid, A, s) : launch_batched_t<2, 64>(grid, A, s);
+// The compiled tile shapes (batched_shape_supported lists them).
+#define FSG_BATCHED_SHAPES(X)                                                                            \
+  X(2, 64, 64, false, 1) X(2, 64, 32, false, 1) X(1, 64, 64, false, 1) X(1, 64, 32, false, 1)        \
+  X(1, 64, 128, false, 1) X(1, 64, 64, true, 1) X(1, 64, 32, true, 1) X(1, 64, 32, false, 2)          \
+  X(1, 128, 64, false, 1) X(1, 128, 32, false, 1)
+
+bool batched_shape_supported(int fb, int eb, int bt, int pk, int minb) {
+#define FSG_X(FB, EB, BT, PK, MINB) \
+  if (fb == FB && eb == EB && bt == BT && pk == (int)PK && minb == MINB) return true;
+  FSG_BATCHED_SHAPES(FSG_X)
+#undef FSG_X
+  return false;
+}
+
+cudaError_t launch_batched(int fb, int eb, int bt, int pk, int minb, int grid, const BatchArgs& A, cudaStream_t s) {
+#define FSG_X(FB, EB, BT, PK, MINB) \
+  if (fb == FB && eb == EB && bt == BT && pk == (int)PK && minb == MINB) return launch_batched_t<FB, EB, BT, PK, MINB>(grid, A, s);
+  FSG_BATCHED_SHAPES(FSG_X)
+#undef FSG_X
+  return cudaErrorInvalidValue;
 }
 
 }  // namespace fsg
@@ -372,7 +422,7 @@ using namespace fsg;
 size_t a256(size_t v) { return (v + 255) & ~size_t(255); }
 
 struct BatchPlanLayout {
-  int fb, eb, chunk, n_items;
+  int fb, eb, bt, pk, minb, chunk, n_items;
   int n_bands[kMaxPhantoms], n_chunks[kMaxPhantoms], item0[kMaxPhantoms];
   int64_t geo0[kMaxPhantoms], max_scat;
   size_t off_src, off_rot, off_tau, off_apod, off_queue, off_tab[kMaxPhantoms], off_partial, off_geo_a, off_geo_b,
@@ -384,8 +434,11 @@ int plan_layout(const FsgProbe* probe, const FsgPhantom* ph, int n_ph, int n_tx,
   L->eb = batched_pad_elements(probe->n_elements);
   // two frequencies per item only fit the 64-element tile's shared memory
   L->fb = (L->eb > 64 || (tu && tu->freqs_per_item == 1)) ? 1 : 2;
+  L->bt = (tu && tu->tile_scatterers > 0) ? tu->tile_scatterers : 64;
+  L->pk = (tu && tu->packed) ? 1 : 0;
+  L->minb = (tu && tu->ctas_per_sm == 2 && batched_shape_supported(L->fb, L->eb, L->bt, L->pk, 2)) ? 2 : 1;
   int64_t chunk = (tu && tu->chunk_scatterers > 0) ? tu->chunk_scatterers : 32768;
-  chunk = ((chunk + kBT - 1) / kBT) * kBT;
+  chunk = ((chunk + L->bt - 1) / L->bt) * L->bt;
   L->chunk = (int)chunk;
   const int E = probe->n_elements, U = probe->n_sub;
   size_t o = 0;
@@ -464,6 +517,15 @@ static int32_t simus_batched_impl(const FsgProbe* probe, const FsgMedium* medium
                                   size_t workspace_bytes, void* stream_ptr) {
   int st = validate_batch(probe, medium, phantoms, n_phantoms, delays, n_tx);
   if (st != FSG_OK) return st;
+  {
+    BatchPlanLayout T;
+    plan_layout(probe, phantoms, n_phantoms, n_tx, tuning, &T, ffd);
+    if (!batched_shape_supported(T.fb, T.eb, T.bt, T.pk, T.minb))
+      return set_error(FSG_EUNSUPPORTED,
+                       "batched tile shape (freqs_per_item %d, elements tile %d, tile_scatterers %d, packed %d) "
+                       "is not compiled into this library",
+                       T.fb, T.eb, T.bt, T.pk);
+  }
   if (ffd) {
     // the per-frequency directivity is a polynomial valid for |k_f seg / 2| <= 2 pi (as in the
     // plain sweep): sub-elements up to two wavelengths of the highest frequency wide
@@ -601,7 +663,9 @@ static int32_t simus_batched_impl(const FsgProbe* probe, const FsgMedium* medium
     const int per_sm = (tuning && tuning->ctas_per_sm > 0) ? tuning->ctas_per_sm : 1;
     int grid = sms * per_sm;
     if (grid > L.n_items) grid = L.n_items;
-    if ((st = check_cuda(launch_batched(L.fb, L.eb, grid, A, s), "batched_kernel launch")) != FSG_OK) return st;
+    if ((st = check_cuda(launch_batched(L.fb, L.eb, L.bt, L.pk, L.minb, grid, A, s), "batched_kernel launch")) !=
+        FSG_OK)
+      return st;
   }
   {
     BatchReduceArgs a;

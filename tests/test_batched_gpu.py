@@ -235,3 +235,43 @@ def test_batched_ffd_wide_subelements_raise():
         BatchedSimus([(g.scatterers, g.rc)], d, wide, g.medium, plans=[plan], full_frequency_directivity=True).run()
     with pytest.raises(NotImplementedError):
         BatchedSimus([(g.scatterers, g.rc)], d, p, g.medium, backend="tc", full_frequency_directivity=True)
+
+
+def _fp32_shapes():
+    from fastsimus_gb300.batched import FP32_SHAPES
+
+    return FP32_SHAPES
+
+
+@pytest.mark.parametrize("shape", _fp32_shapes(), ids=lambda s: "fb{}-e{}-bt{}-pk{}-cta{}".format(*s))
+def test_batched_every_tile_shape_vs_oracle(shape):
+    """Every compiled tile shape of the FP32 batched kernel (frequencies per item, element
+    tile, scatterers per tile, packed FP32x2 register tile, CTAs per SM) against the FP64
+    oracle, with a chunk that is not a multiple of the larger tiles' scatterer count and two
+    phantoms of uneven sizes."""
+    from fastsimus_gb300 import workloads as W
+    from fastsimus_gb300.batched import BatchedSimus, BatchTuning
+
+    fb, eb, bt, pk, cps = shape
+    p, m = (W.cfg1_probe(), W.cfg1_medium()) if eb == 64 else (W.cfg2_probe(), W.cfg2_medium())
+    rng = np.random.default_rng(bt + 7 * fb + pk)
+    phantoms = [(W.uniform_box(rng, n, (-8e-3, 8e-3), (5e-3, 25e-3)), rng.standard_normal(n)) for n in (190, 77)]
+    delays = W.plane_wave_delays(p, m, [-7.0, 0.0, 9.0])
+    apod = np.hanning(p.n_elements) + 0.3
+    b = BatchedSimus(phantoms, delays, p, m, tx_apodization=apod, tuning=BatchTuning(fb, 96, cps, bt, pk))
+    for (s, r), plan, out in zip(phantoms, b.plans, b.run()):
+        rf = np64(out.rf)
+        for t in range(delays.shape[0]):
+            ref = O.simus_compute(s, r, delays[t], plan, p, m, tx_apodization=apod)
+            err = G.rel_l2(rf[:, :, t], ref.rf)
+            assert err < PLAIN_TOL, (shape, t, err)
+
+
+def test_batched_rejects_uncompiled_tile_shape():
+    from fastsimus_gb300 import workloads as W
+    from fastsimus_gb300.batched import BatchedSimus, BatchTuning
+
+    p, m = W.cfg1_probe(), W.cfg1_medium()
+    s, r = W.cfg1_scatterers(100)
+    with pytest.raises(NotImplementedError):  # the packed register tile takes one frequency per item
+        BatchedSimus([(s, r)], W.plane_wave_delays(p, m, [0.0]), p, m, tuning=BatchTuning(2, 8192, 1, 64, 1)).run()
