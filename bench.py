@@ -1039,12 +1039,12 @@ def run_surrogate_workload(args):
                 "frames_per_s_exact": frames / t_exact_full,
                 "green_terms_per_s_surrogate": terms / t_sur_full, "green_terms_per_s_exact": terms / t_exact_full,
                 "fallback_fraction": res["fallback_fraction"], "network_query_share": res["network_query_share"],
-                "units_in_domain": res["units_in_domain"], "units_failed_judge": res["units_failed_judge"],
+                "units_in_domain": res["units_in_domain"], "units_failed_check": res["units_failed_check"],
                 "unit_rel_err_median": res["unit_rel_err_median"], "unit_rel_err_max": res["unit_rel_err_max"],
                 "rf_rel_l2_vs_exact": res["rf_rel_l2_vs_exact"],
                 "sample_scatterers": args.sur_sample,
                 "breakdown_sample_s": {k: res[k] for k in ("t_network_s", "t_exact_outside_domain_s",
-                                                           "t_judge_fallback_s", "t_rx_s")}}
+                                                           "t_check_fallback_s", "t_rx_s")}}
 
     full_s, full_rc = W.cfg4_scatterers(1_000_000, seed=1)
     cfg5 = simus_case(full_s, full_rc, np.linspace(-16.0, 16.0, 75))

@@ -1,7 +1,7 @@
 // Transmit-field surrogate support: the exact transmit field at arbitrary (x, z, f, theta)
 // samples, and the inputs and outputs of the surrogate network.
 //
-// Exact field (the training target and the judge of the network's error).  For a plane wave
+// Exact field (the training target and the check of the network's error).  For a plane wave
 // of steering angle theta on a linear array, delays tau_e = x_e sin(theta) / c - min_e(...)
 // (tx_delay.py:116-189); the complex transmit pressure at (x, z) and frequency f is
 //     p = pulse(f) probe(f) sum_{e,u} apod_e exp(i 2 pi f tau_e) G(x, z, e, u, f)

@@ -1,4 +1,4 @@
-"""Learned transmit-field surrogate with the exact transmit kernel as judge and fallback.
+"""Learned transmit-field surrogate with the exact transmit kernel as error check and fallback.
 
 The network maps (x, z, f, theta) -- a point, a frequency and a plane-wave steering angle --
 to the complex transmit pressure of the array (the pressure inside the pfield step body,
@@ -22,7 +22,7 @@ so many steps are replayed from one CUDA graph.  Inference is the fused tcgen05 
 (fsg_mlp_tc_forward) followed by fsg_surrogate_combine.  PyTorch only holds the buffers.
 
 In simus the network supplies the transmit field at every (scatterer, frequency, firing) inside
-its domain; the exact kernel ``fsg_txfield`` judges each (tile of scatterers, firing) on a few
+its domain; the exact kernel ``fsg_txfield`` checks each (tile of scatterers, firing) on a few
 of its scatterers and recomputes the pairs whose relative L2 error exceeds the tolerance.
 Queries outside the network's domain (points outside the box, steering angles beyond it,
 frequencies outside its band) are computed exactly.  ``simus_with_surrogate`` returns the
@@ -347,10 +347,10 @@ class TxFieldSurrogate:
 
 
 def simus_with_surrogate(sur: TxFieldSurrogate, scat: np.ndarray, rc: np.ndarray, angles_rad, plan, *,
-                         tol: float = 1e-3, tile: int = 64, judges_per_tile: int = 4, exact_reference=True) -> dict:
+                         tol: float = 1e-3, tile: int = 64, checks_per_tile: int = 4, exact_reference=True) -> dict:
     """Simus of one phantom for every firing with the transmit field from the network where the
     query lies in its domain, and from the exact kernel elsewhere.  Every (tile of scatterers,
-    firing) that used the network is judged by the exact kernel on `judges_per_tile` of its
+    firing) that used the network is checked by the exact kernel on `checks_per_tile` of its
     scatterers over all frequencies and recomputed exactly where the relative L2 error exceeds
     `tol`.  The receive contraction with that transmit field is the batched receive kernel.
     Returns RF, timings, the fraction of (tile, firing) units that fell back, the share of
@@ -414,7 +414,7 @@ def simus_with_surrogate(sur: TxFieldSurrogate, scat: np.ndarray, rc: np.ndarray
         tx.view(-1)[idx] = sur.exact(q)
     torch.cuda.synchronize(dev)
     t_exact_part = time.perf_counter() - t0
-    # judge every network-answered (tile, firing) on a few members; recompute failing units exactly
+    # check every network-answered (tile, firing) on a few members; recompute failing units exactly
     t0 = time.perf_counter()
     units = torch.nonzero(use_net)
     errs = torch.zeros(0, device=dev)
@@ -423,15 +423,15 @@ def simus_with_surrogate(sur: TxFieldSurrogate, scat: np.ndarray, rc: np.ndarray
         n_u = units.shape[0]
         lo = units[:, 0] * tile
         last = torch.clamp(lo + tile, max=S) - 1
-        frac = torch.linspace(0.0, 1.0, judges_per_tile, dtype=torch.float64, device=dev)
-        jrows = (lo[:, None] + ((last - lo)[:, None].double() * frac[None, :]).round().long())  # (units, judges)
-        q = torch.empty(n_u, judges_per_tile, F, 4, dtype=torch.float64, device=dev)
+        frac = torch.linspace(0.0, 1.0, checks_per_tile, dtype=torch.float64, device=dev)
+        jrows = (lo[:, None] + ((last - lo)[:, None].double() * frac[None, :]).round().long())  # (units, checks)
+        q = torch.empty(n_u, checks_per_tile, F, 4, dtype=torch.float64, device=dev)
         q[..., 0] = sc[jrows, 0][..., None]
         q[..., 1] = sc[jrows, 1][..., None]
         q[..., 2] = f[None, None, :]
         q[..., 3] = th[units[:, 1]][:, None, None]
-        ex = sur.exact(q.view(-1, 4)).view(n_u, judges_per_tile, F)
-        got = tx[jrows, :, units[:, 1][:, None]]  # (units, judges, F)
+        ex = sur.exact(q.view(-1, 4)).view(n_u, checks_per_tile, F)
+        got = tx[jrows, :, units[:, 1][:, None]]  # (units, checks, F)
         errs = torch.linalg.vector_norm((got - ex).reshape(n_u, -1), dim=1) / \
             torch.linalg.vector_norm(ex.reshape(n_u, -1), dim=1)
         failed_units = units[errs > tol]
@@ -444,7 +444,7 @@ def simus_with_surrogate(sur: TxFieldSurrogate, scat: np.ndarray, rc: np.ndarray
     failed = int(failed_units.shape[0])
     errs = errs.cpu().numpy()
     torch.cuda.synchronize(dev)
-    t_judge = time.perf_counter() - t0
+    t_check = time.perf_counter() - t0
     # receive contraction with that transmit field
     bs = BatchedSimus([(scat, rc)], delays, p, m, plans=[plan], backend="fp32", tuning=BatchTuning(2, 32768, 1))
     t0 = time.perf_counter()
@@ -456,9 +456,9 @@ def simus_with_surrogate(sur: TxFieldSurrogate, scat: np.ndarray, rc: np.ndarray
     n_units = n_tiles * T
     fallback_units = n_units - int(use_net.sum()) + failed
     res = {"rf": bs.rfs[0].clone(), "t_network_s": t_net, "t_exact_outside_domain_s": t_exact_part,
-           "t_judge_fallback_s": t_judge, "t_rx_s": t_rx,
-           "t_surrogate_total_s": t_net + t_exact_part + t_judge + t_rx, "units": n_units,
-           "units_in_domain": int(use_net.sum()), "units_failed_judge": failed,
+           "t_check_fallback_s": t_check, "t_rx_s": t_rx,
+           "t_surrogate_total_s": t_net + t_exact_part + t_check + t_rx, "units": n_units,
+           "units_in_domain": int(use_net.sum()), "units_failed_check": failed,
            "fallback_fraction": fallback_units / max(1, n_units),
            "network_query_share": (n_net - n_fail_queries) / max(1, S * F * T),
            "unit_rel_err_median": float(np.median(errs)) if errs.size else None,

@@ -153,7 +153,7 @@ def test_training_meets_the_tolerance_over_the_box(trained):
 
 def test_simus_with_the_trained_surrogate_records_its_gain(trained):
     """A phantom inside the training box, firings inside its angle range: the network answers
-    the queries inside its band, the judge accepts (tile, firing) units at 1e-3, and the RF
+    the queries inside its band, the exact check accepts (tile, firing) units at 1e-3, and the RF
     agrees with the exact batched sweep; the timings record the gain against the exact path
     (below 1 here: the batched sweep shares each Green's term between the firings, which a
     per-query network cannot)."""
