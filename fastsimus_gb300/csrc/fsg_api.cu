@@ -238,11 +238,11 @@ static int simus_grid(int n_bands, int64_t chunk_tiles, int num_sms) {
 // kTxAnchor frequencies, else of kAnchor, such that the shared memory fits.  False when no
 // shape fits (simus_band_kernel takes those probes).
 static bool stash_shape(int E, int U, int ffd, SweepConfig* c) {
-  if (U < 1 || U > 4) return false;
-  const int spe = U == 1 ? 1 : (U == 2 ? 2 : 4);
+  if (U < 1 || U > 8) return false;
+  const int spe = U == 1 ? 1 : (U == 2 ? 2 : (U <= 4 ? 4 : 8));
   const int epl = kSrcPerThread / spe;
-  // the warp-specialised kernel: E = 64, 128 (any U) or 256 (U <= 2); 128 transmit threads
-  if ((E == 64 || E == 128 || (E == 256 && U <= 2))) {
+  // the warp-specialised kernel: E = 64, 128 (U <= 4) or 256 (U <= 2); 128 transmit threads
+  if ((E == 64 || E == 128 || E == 256) && U <= (E == 256 ? 2 : 4)) {
     int gn = E * spe / kSrcPerThread;
     if (gn < 4) gn = 4;
     const int st = 128 / gn, fb = E > 128 ? 32 : 64;
@@ -391,7 +391,7 @@ extern "C" int32_t fsg_simus(const FsgProbe* probe, const FsgMedium* medium, con
                              size_t workspace_bytes, void* stream_ptr) {
   int st = validate_common(probe, medium, plan, ffd);
   if (st != FSG_OK) return st;
-  if (probe->n_sub > 4) return set_error(FSG_EUNSUPPORTED, "n_sub = %d > 4 is not supported by this library", probe->n_sub);
+  if (probe->n_sub > 8) return set_error(FSG_EUNSUPPORTED, "n_sub = %d > 8 is not supported by this library", probe->n_sub);
   if (n_scat < 0) return set_error(FSG_EINVAL, "n_scat must be >= 0");
   if (n_scat > 0 && (!scat_xz || !rc)) return set_error(FSG_EINVAL, "scatterer and rc pointers must be non-NULL");
   if (!delays) return set_error(FSG_EINVAL, "delays pointer must be non-NULL");
@@ -407,6 +407,11 @@ extern "C" int32_t fsg_simus(const FsgProbe* probe, const FsgMedium* medium, con
   const int E = probe->n_elements, U = probe->n_sub, F = plan->n_freq;
   // the default chunking, or smaller chunks when the caller's workspace is smaller
   SweepConfig c = simus_config(E, U, F, n_scat, sms, kGeoCacheBudget, ffd);
+  if (c.kind == 0 && U > 4)
+    return set_error(FSG_EUNSUPPORTED,
+                     "n_sub = %d > 4 is supported for probes whose 8-slot elements map onto 32 lanes "
+                     "(n_elements <= 64); got n_elements = %d",
+                     U, E);
   if (workspace && workspace_bytes < simus_ws_size(c, E, U, F)) {
     const size_t fixed = simus_ws_size(c, E, U, F) - align256((size_t)c.chunk_tiles * c.geo_bytes);
     if (workspace_bytes > fixed) c = simus_config(E, U, F, n_scat, sms, workspace_bytes - fixed - 256, ffd);

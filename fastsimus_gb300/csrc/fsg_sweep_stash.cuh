@@ -28,6 +28,10 @@
 
 namespace fsg {
 
+// Source slots per element of a lane: 1, 2, 4 (U = 3 and 4) or 8 (U = 5 to 8, the kernels
+// instantiated with U = 8 and the runtime count).
+__host__ __device__ constexpr int stash_spe(int U) { return U == 1 ? 1 : (U == 2 ? 2 : (U <= 4 ? 4 : 8)); }
+
 // Receive over one stash sub-block: Ys[sb FS + j][e] += sum_s stash[s][j][e] W[s][j] for the
 // NJ frequencies j of each item (e, j0).  A warp takes consecutive elements: the stash reads
 // are contiguous and the W reads are broadcasts.
@@ -79,10 +83,10 @@ __device__ __forceinline__ void stash_transmit(float2 (&Gr)[kSrcPerThread / 2], 
                                                const float2 (&Si)[kSrcPerThread / 2],
                                                const float2 (&Sn)[kSrcPerThread / 2],
                                                const float2 (&Dh)[FFD ? kSrcPerThread / 2 : 1],
-                                               const float (&wk)[kSrcPerThread / ((U == 1) ? 1 : (U == 2 ? 2 : 4))],
+                                               const float (&wk)[kSrcPerThread / stash_spe(U)],
                                                float2* __restrict__ stash_row, int ep, int g, int E,
                                                const float* __restrict__ kb_sb, float2 (&v)[kStashFreqs]) {
-  constexpr int SPE = (U == 1) ? 1 : (U == 2 ? 2 : 4);
+  constexpr int SPE = stash_spe(U);
   constexpr int EPL = kSrcPerThread / SPE;
   constexpr int kPairs = kSrcPerThread / 2;
   constexpr int FS = kStashFreqs;
@@ -115,15 +119,27 @@ __device__ __forceinline__ void stash_transmit(float2 (&Gr)[kSrcPerThread / 2], 
           m = make_float2(Gr[k].x + Gr[k].y, Gi[k].x + Gi[k].y);
         }
       } else {
+        // SPE / 2 pairs per element (the slots past the element's sub-elements hold zeros)
+        constexpr int PPE = SPE / 2;
         float2 tr, ti;
         if constexpr (FFD) {
-          const float2 d0 = sinc_poly2(__fmul2_rn(Dh[2 * k], kk));
-          const float2 d1 = sinc_poly2(__fmul2_rn(Dh[2 * k + 1], kk));
-          tr = __ffma2_rn(Gr[2 * k + 1], d1, __fmul2_rn(Gr[2 * k], d0));
-          ti = __ffma2_rn(Gi[2 * k + 1], d1, __fmul2_rn(Gi[2 * k], d0));
+          const float2 d0 = sinc_poly2(__fmul2_rn(Dh[PPE * k], kk));
+          tr = __fmul2_rn(Gr[PPE * k], d0);
+          ti = __fmul2_rn(Gi[PPE * k], d0);
+#pragma unroll
+          for (int q = 1; q < PPE; ++q) {
+            const float2 d = sinc_poly2(__fmul2_rn(Dh[PPE * k + q], kk));
+            tr = __ffma2_rn(Gr[PPE * k + q], d, tr);
+            ti = __ffma2_rn(Gi[PPE * k + q], d, ti);
+          }
         } else {
-          tr = __fadd2_rn(Gr[2 * k], Gr[2 * k + 1]);
-          ti = __fadd2_rn(Gi[2 * k], Gi[2 * k + 1]);
+          tr = Gr[PPE * k];
+          ti = Gi[PPE * k];
+#pragma unroll
+          for (int q = 1; q < PPE; ++q) {
+            tr = __fadd2_rn(tr, Gr[PPE * k + q]);
+            ti = __fadd2_rn(ti, Gi[PPE * k + q]);
+          }
         }
         m = make_float2(tr.x + tr.y, ti.x + ti.y);
       }
@@ -155,7 +171,7 @@ __device__ __forceinline__ void stash_transmit(float2 (&Gr)[kSrcPerThread / 2], 
 
 template <int U, int GN, bool FFD>
 __global__ void __launch_bounds__(kThreads, 1) simus_stash_kernel(const BandArgs A) {
-  constexpr int SPE = (U == 1) ? 1 : (U == 2 ? 2 : 4);  // source slots per element (U = 3 pads one)
+  constexpr int SPE = stash_spe(U);  // source slots per element (U = 3 pads one, U = 5..7 pad to 8)
   constexpr int EPL = kSrcPerThread / SPE;             // element slots per lane
   constexpr int kPairs = kSrcPerThread / 2;
   constexpr int FS = kStashFreqs;
@@ -259,7 +275,7 @@ __global__ void __launch_bounds__(kThreads, 1) simus_stash_kernel(const BandArgs
           gv[h] = make_float2(0.f, 0.f);
           sv[h] = make_float2(0.f, 0.f);
           dv[h] = 0.f;
-          if (uu < U && e < E) {
+          if (uu < (U == 8 ? A.U : U) && e < E) {
             const int idx = uu * L.g.plane + e * L.g.pitch + sl;
             gv[h] = cmul(anchor_value(b_rhi[idx], b_rlo[idx], b_amp[idx], k0, a0), dph[e]);
             sv[h] = cmul(b_st[idx], dstep[e]);
@@ -593,6 +609,10 @@ static cudaError_t launch_simus_stash_u(int U, const SweepConfig& c, const BandA
     case 2: return launch_simus_stash_gn<2, FFD>(c, A, s);
     case 3: return launch_simus_stash_gn<3, FFD>(c, A, s);
     case 4: return launch_simus_stash_gn<4, FFD>(c, A, s);
+    case 5:
+    case 6:
+    case 7:
+    case 8: return launch_simus_stash_gn<8, FFD>(c, A, s);  // the runtime count pads to 8 slots
     default: return cudaErrorInvalidValue;
   }
 }

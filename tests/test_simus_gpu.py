@@ -229,12 +229,14 @@ def test_full_frame_plan_matches_reference_golden():
 @pytest.mark.parametrize("n_elements,splitting,ffd,baffle", [
     (256, 1, False, "soft"), (256, 2, True, "rigid"), (128, 1, False, 1.5), (128, 3, False, "soft"),
     (128, 4, True, "soft"), (64, 4, False, "rigid"), (64, 1, True, "soft"),
-    (192, 2, False, "soft"), (48, 2, True, 1.5), (160, 3, False, "soft")])
+    (192, 2, False, "soft"), (48, 2, True, 1.5), (160, 3, False, "soft"),
+    (64, 6, False, "soft"), (48, 8, True, "rigid"), (32, 5, False, 1.5)])
 def test_sweep_kernel_shapes_vs_oracle(n_elements, splitting, ffd, baffle):
     """Every sweep kernel against the FP64 oracle: the warp-specialised stash kernel (64, 128
     and 256 elements, one to four sub-elements, with and without full-frequency directivity),
-    the single-role stash kernel (192 and 48 elements) and the re-generating band kernel (160
-    elements x 3 sub-elements, whose 16-slot lanes the stash kernels cannot map)."""
+    the single-role stash kernel (192 and 48 elements; five to eight sub-elements on probes of
+    up to 64 elements) and the re-generating band kernel (160 elements x 3 sub-elements, whose
+    16-slot lanes the stash kernels cannot map)."""
     import fastsimus_gb300 as F
     from fastsimus_gb300.params import TransducerParams
 
@@ -254,3 +256,15 @@ def test_sweep_kernel_shapes_vs_oracle(n_elements, splitting, ffd, baffle):
     err = G.rel_l2(got, ref.rf)
     print(f"E={n_elements} U={splitting} ffd={ffd} baffle={baffle}: relL2 {err:.2e}")
     assert err < PLAIN_TOL
+
+
+def test_more_than_four_sub_elements_on_a_wide_probe_raise():
+    """Five or more sub-elements are mapped for probes of up to 64 elements; a 128-element probe
+    with six raises instead of running a kernel that cannot hold it."""
+    import fastsimus_gb300 as F
+    from fastsimus_gb300.params import TransducerParams
+
+    p = TransducerParams(freq_center=4e6, pitch=3e-4, n_elements=128, width=2.7e-4, bandwidth=0.6)
+    s = np.array([[0.0, 0.02]])
+    with pytest.raises(NotImplementedError):
+        F.simus(s, np.ones(1), np.zeros(128), p, element_splitting=6)
