@@ -1,7 +1,7 @@
 """Public pfield API, drop-in for the reference's ``fast_simus.pfield`` module (pfield.py:41-475).
 
-Returns the RMS pressure field as a float32 torch tensor of shape ``positions.shape[:-1]`` on
-the current CUDA device.  ``PfieldStrategy`` keeps the reference's values and adds ``GB300``;
+Returns the RMS pressure field as a float64 torch tensor (the reference's dtype; computed in
+FP32 with double-float phases) of shape ``positions.shape[:-1]`` on the current CUDA device.  ``PfieldStrategy`` keeps the reference's values and adds ``GB300``;
 ``None`` selects it.  VECTORIZED/SCAN (CPU) and METAL (Apple) raise ``NotImplementedError``.
 """
 
@@ -67,7 +67,7 @@ def pfield_compute(positions, delays, plan: PfieldPlan, params: TransducerParams
                             a.data_ptr() if a is not None else None, int(bool(full_frequency_directivity)),
                             out.data_ptr(), ws.data_ptr(), ws.numel(), _device.stream_handle(device))
     _native.check(st)
-    return out.reshape(grid_shape)
+    return out.reshape(grid_shape).to(torch.float64)
 
 
 def pfield(positions, delays, params: TransducerParams, medium: MediumParams = _DEFAULT_MEDIUM, *,

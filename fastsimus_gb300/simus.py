@@ -2,8 +2,10 @@
 
 Same names, arguments and return types (``SimusResult(rf, spectrum)``); the frequency sweep
 runs in libfsgb300.so on the GPU.  Inputs may be NumPy arrays (copied to the current CUDA
-device) or torch tensors; results are torch tensors on that device: ``rf`` float32
-(n_samples, E) and ``spectrum`` complex64 (n_freq_full, E).
+device) or torch tensors; results are torch tensors on that device with the reference's
+dtypes: ``rf`` float64 (n_samples, E) and ``spectrum`` complex128 (n_freq_full, E).  The
+values are computed in FP32 with double-float phases (relative L2 ~1e-6 against the FP64
+path) and widened on the device; ``BatchedSimus`` keeps float32 / complex64.
 
 ``SimusStrategy`` keeps the reference's values and adds ``GB300``; ``None`` and ``CUDA`` select
 the GB300 kernels.  The CPU strategies (PYTHON, SCAN) and Apple's METAL are not part of this
@@ -35,7 +37,8 @@ class SimusStrategy(StrEnum):
 
 
 class SimusResult(NamedTuple):
-    """rf: (n_samples, n_elements) float32; spectrum: (n_freq_full, n_elements) complex64."""
+    """rf: (n_samples, n_elements) float64; spectrum: (n_freq_full, n_elements) complex128 (the
+    batched API returns float32 / complex64 with a trailing firing axis)."""
 
     rf: torch.Tensor
     spectrum: torch.Tensor
@@ -144,7 +147,7 @@ def simus_compute(scatterers, rc, delays, plan: SimusPlan, params: TransducerPar
     full = _launch_simus(scat, r, d, a, plan, params, medium, full_frequency_directivity,
                          _native.FSG_OUT_FULL_CORRECTED, device)
     rf = irfft_and_threshold(full, plan, k_first=int(plan.freq_idx_start), k_count=int(plan.selected_freqs.shape[0]))
-    return SimusResult(rf=rf, spectrum=full)
+    return SimusResult(rf=rf.to(torch.float64), spectrum=full.to(torch.complex128))
 
 
 def simus(scatterers, rc, delays, params: TransducerParams, medium: MediumParams = _DEFAULT_MEDIUM, *,
