@@ -84,7 +84,7 @@ class FsgMlpTrain(ctypes.Structure):
 class FsgBatchTuning(ctypes.Structure):
     _fields_ = [("freqs_per_item", ctypes.c_int32), ("chunk_scatterers", ctypes.c_int32),
                 ("ctas_per_sm", ctypes.c_int32), ("tile_scatterers", ctypes.c_int32), ("packed", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 3)]
+                ("threads_per_cta", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
 
 
 FSG_DAS_LINEAR, FSG_DAS_NEAREST = range(2)

@@ -44,6 +44,7 @@ class BatchTuning:
     ctas_per_sm: int = 1
     tile_scatterers: int = 64
     packed: int = 0
+    threads_per_cta: int = 256
 
     @staticmethod
     def default(backend: str) -> "BatchTuning":
@@ -51,12 +52,15 @@ class BatchTuning:
 
     def to_c(self) -> _native.FsgBatchTuning:
         return _native.FsgBatchTuning(self.freqs_per_item, self.chunk_scatterers, self.ctas_per_sm,
-                                      self.tile_scatterers, self.packed)
+                                      self.tile_scatterers, self.packed, self.threads_per_cta)
 
 
-# (freqs_per_item, elements tile, tile_scatterers, packed, ctas_per_sm) compiled into batched_kernel
-FP32_SHAPES = ((2, 64, 64, 0, 1), (2, 64, 32, 0, 1), (1, 64, 64, 0, 1), (1, 64, 32, 0, 1), (1, 64, 128, 0, 1),
-               (1, 64, 64, 1, 1), (1, 64, 32, 1, 1), (1, 64, 32, 0, 2), (1, 128, 64, 0, 1), (1, 128, 32, 0, 1))
+# (freqs_per_item, elements tile, tile_scatterers, packed, ctas_per_sm, threads_per_cta) compiled
+# into batched_kernel
+FP32_SHAPES = ((2, 64, 64, 0, 1, 256), (2, 64, 32, 0, 1, 256), (1, 64, 64, 0, 1, 256), (1, 64, 32, 0, 1, 256),
+               (1, 64, 128, 0, 1, 256), (1, 64, 64, 1, 1, 256), (1, 64, 32, 1, 1, 256), (1, 64, 32, 0, 2, 256),
+               (1, 128, 64, 0, 1, 256), (1, 128, 32, 0, 1, 256), (2, 64, 64, 0, 1, 512), (1, 64, 64, 0, 1, 512),
+               (1, 64, 128, 0, 1, 512), (1, 128, 64, 0, 1, 512))
 
 
 def fp32_search_space(n_elements: int, total_scatterers: int) -> list[BatchTuning]:
@@ -65,7 +69,8 @@ def fp32_search_space(n_elements: int, total_scatterers: int) -> list[BatchTunin
     eb = 64 if n_elements <= 64 else 128
     chunks = sorted({c for c in (8192, 16384, 32768, 65536) if c < 2 * max(total_scatterers, 64)} or {8192})
     chunks = [chunks[0], chunks[-1]] if len(chunks) > 1 else chunks
-    return [BatchTuning(fb, c, cps, bt, pk) for fb, e, bt, pk, cps in FP32_SHAPES if e == eb for c in chunks]
+    return [BatchTuning(fb, c, cps, bt, pk, nth) for fb, e, bt, pk, cps, nth in FP32_SHAPES if e == eb
+            for c in chunks]
 
 
 def shared_plan(scatterers, rc, delays_list, params: TransducerParams, medium: MediumParams, **plan_kw) -> SimusPlan:

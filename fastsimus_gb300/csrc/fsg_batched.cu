@@ -68,16 +68,18 @@ __device__ __forceinline__ float2 pk_cfma(float2 a, float4 b, float2 acc) {
   return __ffma2_rn(make_float2(a.y, a.y), make_float2(b.z, b.w), acc);
 }
 
-// FB frequencies per item, EB padded elements, BT scatterers per tile; the transmit register
-// tile is BT/16 scatterer rows x 5 transmits per thread, the receive tile EB/16 element rows x
-// 5 transmits.  PK: the complex MACs on the FP32x2 pipe with (b, conj-swapped b) operands in
-// shared memory.  MINB: CTAs per SM the register budget is cut for.
-template <int FB, int EB, int BT, bool PK, int MINB>
-__global__ void __launch_bounds__(kThreads, MINB) batched_kernel(const __grid_constant__ BatchArgs A) {
+// FB frequencies per item, EB padded elements, BT scatterers per tile, NTH threads (256 or 512:
+// 4 or 8 row groups of warps x 2 column groups); the transmit register tile is
+// BT / (4 NTH / 64) scatterer rows x 5 transmits per thread, the receive tile EB / (4 NTH / 64)
+// element rows x 5 transmits.  PK: the complex MACs on the FP32x2 pipe with (b, conj-swapped
+// b) operands in shared memory.  MINB: CTAs per SM the register budget is cut for.
+template <int FB, int EB, int BT, bool PK, int MINB, int NTH>
+__global__ void __launch_bounds__(NTH, MINB) batched_kernel(const __grid_constant__ BatchArgs A) {
   extern __shared__ __align__(16) unsigned char sm[];
   constexpr int kGmPitch = gm_pitch(EB);
-  constexpr int kRows = EB / 16;                                     // receive rows per thread
-  constexpr int kTRows = BT / 16;                                    // transmit rows per thread
+  constexpr int NWM = NTH / 64;                                      // row groups of warps
+  constexpr int kRows = EB / (4 * NWM);                              // receive rows per thread
+  constexpr int kTRows = BT / (4 * NWM);                             // transmit rows per thread
   using BOp = typename std::conditional<PK, float4, float2>::type;  // a B-operand entry
   float2* Gm = reinterpret_cast<float2*>(sm);                       // [FB][BT][kGmPitch]
   BOp* D = reinterpret_cast<BOp*>(Gm + FB * BT * kGmPitch);          // [FB][EB][kWPitch]
@@ -86,7 +88,7 @@ __global__ void __launch_bounds__(kThreads, MINB) batched_kernel(const __grid_co
   __shared__ int s_item;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wm = warp & 3, wn = warp >> 2, lm = lane & 3, ln = lane >> 2;
+  const int wm = warp % NWM, wn = warp / NWM, lm = lane & 3, ln = lane >> 2;
   const int E = A.E, U = A.U, T = A.n_tx;
 
   for (;;) {
@@ -108,7 +110,7 @@ __global__ void __launch_bounds__(kThreads, MINB) batched_kernel(const __grid_co
     const int64_t s_end = min(P.n_scat, s_begin + A.chunk);
 
     // --- transmit matrices D[f][e][t] for the band (exact, per item) ---
-    for (int i = tid; i < FB * EB * kBTX; i += kThreads) {
+    for (int i = tid; i < FB * EB * kBTX; i += NTH) {
       const int f = i / (EB * kBTX), r = i % (EB * kBTX), e = r / kBTX, t = r % kBTX;
       float2 v = make_float2(0.f, 0.f);
       if (f < nf && e < E && t < T) {
@@ -158,7 +160,7 @@ __global__ void __launch_bounds__(kThreads, MINB) batched_kernel(const __grid_co
       __syncthreads();
       // --- Green's matrix Gm[f][s][e] for the tile: thread (e, s-group of BT * EB / 256) ---
       {
-        constexpr int kSpg = BT * EB / kThreads;
+        constexpr int kSpg = BT * EB / NTH;
         const int e = tid % EB;
         const int sg = tid / EB;
         for (int k = 0; k < kSpg; ++k) {
@@ -196,7 +198,7 @@ __global__ void __launch_bounds__(kThreads, MINB) batched_kernel(const __grid_co
         const float2* G = Gm + f * BT * kGmPitch;
         if (A.tx_in) {
           // transmit field supplied by the caller (already includes pulse * probe): W = rc * p
-          for (int i = tid; i < BT * kBTX; i += kThreads) {
+          for (int i = tid; i < BT * kBTX; i += NTH) {
             const int sl = i / kBTX, t = i % kBTX;
             const int64_t sg = t0 + sl;
             float2 v = make_float2(0.f, 0.f);
@@ -221,7 +223,7 @@ __global__ void __launch_bounds__(kThreads, MINB) batched_kernel(const __grid_co
             float2 a[kTRows];
             BOp b[5];
   #pragma unroll
-            for (int i = 0; i < kTRows; ++i) a[i] = G[(wm * (BT / 4) + lm + 4 * i) * kGmPitch + e];
+            for (int i = 0; i < kTRows; ++i) a[i] = G[(wm * (BT / NWM) + lm + 4 * i) * kGmPitch + e];
   #pragma unroll
             for (int j = 0; j < 5; ++j) b[j] = Df[e * kWPitch + wn * 40 + ln * 5 + j];
   #pragma unroll
@@ -235,7 +237,7 @@ __global__ void __launch_bounds__(kThreads, MINB) batched_kernel(const __grid_co
           // W[s][t] = rc_s * pulse * probe * P
   #pragma unroll
           for (int i = 0; i < kTRows; ++i) {
-            const int s = wm * (BT / 4) + lm + 4 * i;
+            const int s = wm * (BT / NWM) + lm + 4 * i;
             const float w = rcs[s];
             const float2 sc = make_float2(w * pp[f].x, w * pp[f].y);
   #pragma unroll
@@ -253,7 +255,7 @@ __global__ void __launch_bounds__(kThreads, MINB) batched_kernel(const __grid_co
           float2 a[kRows];
           BOp b[5];
 #pragma unroll
-          for (int i = 0; i < kRows; ++i) a[i] = G[s * kGmPitch + wm * (EB / 4) + lm + 4 * i];
+          for (int i = 0; i < kRows; ++i) a[i] = G[s * kGmPitch + wm * (EB / NWM) + lm + 4 * i];
 #pragma unroll
           for (int j = 0; j < 5; ++j) b[j] = W[s * kWPitch + wn * 40 + ln * 5 + j];
 #pragma unroll
@@ -275,7 +277,7 @@ __global__ void __launch_bounds__(kThreads, MINB) batched_kernel(const __grid_co
       for (int i = 0; i < kRows; ++i)
 #pragma unroll
         for (int j = 0; j < 5; ++j) {
-          const int e = wm * (EB / 4) + lm + 4 * i, t = wn * 40 + ln * 5 + j;
+          const int e = wm * (EB / NWM) + lm + 4 * i, t = wn * 40 + ln * 5 + j;
           out[((size_t)f * kBTX + t) * EB + e] = Y[f][i][j];
         }
   }
@@ -377,33 +379,37 @@ size_t batched_smem_bytes(int fb, int eb, int bt, int pk) {
 
 int batched_pad_elements(int n_elements) { return n_elements <= 64 ? 64 : 128; }
 
-template <int FB, int EB, int BT, bool PK, int MINB>
+template <int FB, int EB, int BT, bool PK, int MINB, int NTH>
 static cudaError_t launch_batched_t(int grid, const BatchArgs& A, cudaStream_t s) {
   const size_t smem = batched_smem_bytes(FB, EB, BT, PK);
-  auto k = batched_kernel<FB, EB, BT, PK, MINB>;
+  auto k = batched_kernel<FB, EB, BT, PK, MINB, NTH>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k<<<grid, kThreads, smem, s>>>(A);
+  k<<<grid, NTH, smem, s>>>(A);
   return cudaGetLastError();
 }
 
 // The compiled tile shapes (batched_shape_supported lists them).
 #define FSG_BATCHED_SHAPES(X)                                                                            \
-  X(2, 64, 64, false, 1) X(2, 64, 32, false, 1) X(1, 64, 64, false, 1) X(1, 64, 32, false, 1)        \
-  X(1, 64, 128, false, 1) X(1, 64, 64, true, 1) X(1, 64, 32, true, 1) X(1, 64, 32, false, 2)          \
-  X(1, 128, 64, false, 1) X(1, 128, 32, false, 1)
+  X(2, 64, 64, false, 1, 256) X(2, 64, 32, false, 1, 256) X(1, 64, 64, false, 1, 256)                  \
+  X(1, 64, 32, false, 1, 256) X(1, 64, 128, false, 1, 256) X(1, 64, 64, true, 1, 256)                 \
+  X(1, 64, 32, true, 1, 256) X(1, 64, 32, false, 2, 256) X(1, 128, 64, false, 1, 256)                 \
+  X(1, 128, 32, false, 1, 256) X(2, 64, 64, false, 1, 512) X(1, 64, 64, false, 1, 512)                \
+  X(1, 64, 128, false, 1, 512) X(1, 128, 64, false, 1, 512)
 
-bool batched_shape_supported(int fb, int eb, int bt, int pk, int minb) {
-#define FSG_X(FB, EB, BT, PK, MINB) \
-  if (fb == FB && eb == EB && bt == BT && pk == (int)PK && minb == MINB) return true;
+bool batched_shape_supported(int fb, int eb, int bt, int pk, int minb, int nth) {
+#define FSG_X(FB, EB, BT, PK, MINB, NTH) \
+  if (fb == FB && eb == EB && bt == BT && pk == (int)PK && minb == MINB && nth == NTH) return true;
   FSG_BATCHED_SHAPES(FSG_X)
 #undef FSG_X
   return false;
 }
 
-cudaError_t launch_batched(int fb, int eb, int bt, int pk, int minb, int grid, const BatchArgs& A, cudaStream_t s) {
-#define FSG_X(FB, EB, BT, PK, MINB) \
-  if (fb == FB && eb == EB && bt == BT && pk == (int)PK && minb == MINB) return launch_batched_t<FB, EB, BT, PK, MINB>(grid, A, s);
+cudaError_t launch_batched(int fb, int eb, int bt, int pk, int minb, int nth, int grid, const BatchArgs& A,
+                           cudaStream_t s) {
+#define FSG_X(FB, EB, BT, PK, MINB, NTH)                                                  \
+  if (fb == FB && eb == EB && bt == BT && pk == (int)PK && minb == MINB && nth == NTH) \
+    return launch_batched_t<FB, EB, BT, PK, MINB, NTH>(grid, A, s);
   FSG_BATCHED_SHAPES(FSG_X)
 #undef FSG_X
   return cudaErrorInvalidValue;
@@ -422,7 +428,7 @@ using namespace fsg;
 size_t a256(size_t v) { return (v + 255) & ~size_t(255); }
 
 struct BatchPlanLayout {
-  int fb, eb, bt, pk, minb, chunk, n_items;
+  int fb, eb, bt, pk, minb, nth, chunk, n_items;
   int n_bands[kMaxPhantoms], n_chunks[kMaxPhantoms], item0[kMaxPhantoms];
   int64_t geo0[kMaxPhantoms], max_scat;
   size_t off_src, off_rot, off_tau, off_apod, off_queue, off_tab[kMaxPhantoms], off_partial, off_geo_a, off_geo_b,
@@ -436,7 +442,8 @@ int plan_layout(const FsgProbe* probe, const FsgPhantom* ph, int n_ph, int n_tx,
   L->fb = (L->eb > 64 || (tu && tu->freqs_per_item == 1)) ? 1 : 2;
   L->bt = (tu && tu->tile_scatterers > 0) ? tu->tile_scatterers : 64;
   L->pk = (tu && tu->packed) ? 1 : 0;
-  L->minb = (tu && tu->ctas_per_sm == 2 && batched_shape_supported(L->fb, L->eb, L->bt, L->pk, 2)) ? 2 : 1;
+  L->nth = (tu && tu->threads_per_cta > 0) ? tu->threads_per_cta : 256;
+  L->minb = (tu && tu->ctas_per_sm == 2 && batched_shape_supported(L->fb, L->eb, L->bt, L->pk, 2, L->nth)) ? 2 : 1;
   int64_t chunk = (tu && tu->chunk_scatterers > 0) ? tu->chunk_scatterers : 32768;
   chunk = ((chunk + L->bt - 1) / L->bt) * L->bt;
   L->chunk = (int)chunk;
@@ -520,11 +527,11 @@ static int32_t simus_batched_impl(const FsgProbe* probe, const FsgMedium* medium
   {
     BatchPlanLayout T;
     plan_layout(probe, phantoms, n_phantoms, n_tx, tuning, &T, ffd);
-    if (!batched_shape_supported(T.fb, T.eb, T.bt, T.pk, T.minb))
+    if (!batched_shape_supported(T.fb, T.eb, T.bt, T.pk, T.minb, T.nth))
       return set_error(FSG_EUNSUPPORTED,
-                       "batched tile shape (freqs_per_item %d, elements tile %d, tile_scatterers %d, packed %d) "
-                       "is not compiled into this library",
-                       T.fb, T.eb, T.bt, T.pk);
+                       "batched tile shape (freqs_per_item %d, elements tile %d, tile_scatterers %d, packed %d, "
+                       "threads %d) is not compiled into this library",
+                       T.fb, T.eb, T.bt, T.pk, T.nth);
   }
   if (ffd) {
     // the per-frequency directivity is a polynomial valid for |k_f seg / 2| <= 2 pi (as in the
@@ -663,8 +670,8 @@ static int32_t simus_batched_impl(const FsgProbe* probe, const FsgMedium* medium
     const int per_sm = (tuning && tuning->ctas_per_sm > 0) ? tuning->ctas_per_sm : 1;
     int grid = sms * per_sm;
     if (grid > L.n_items) grid = L.n_items;
-    if ((st = check_cuda(launch_batched(L.fb, L.eb, L.bt, L.pk, L.minb, grid, A, s), "batched_kernel launch")) !=
-        FSG_OK)
+    if ((st = check_cuda(launch_batched(L.fb, L.eb, L.bt, L.pk, L.minb, L.nth, grid, A, s),
+                         "batched_kernel launch")) != FSG_OK)
       return st;
   }
   {

@@ -77,9 +77,10 @@ size_t batched_smem_bytes(int fb, int eb, int bt, int pk);
 // Padded element count of the FP32 batched kernel's tiles (64 or 128).
 int batched_pad_elements(int n_elements);
 __global__ void batched_geometry_kernel(const __grid_constant__ BatchArgs A);
-// Launches batched_kernel<fb, eb, bt, pk, minb>; cudaErrorInvalidValue for a shape that is not compiled.
-cudaError_t launch_batched(int fb, int eb, int bt, int pk, int minb, int grid, const BatchArgs& A, cudaStream_t s);
-bool batched_shape_supported(int fb, int eb, int bt, int pk, int minb);
+// Launches batched_kernel<fb, eb, bt, pk, minb, nth>; cudaErrorInvalidValue for a shape that is not compiled.
+cudaError_t launch_batched(int fb, int eb, int bt, int pk, int minb, int nth, int grid, const BatchArgs& A,
+                           cudaStream_t s);
+bool batched_shape_supported(int fb, int eb, int bt, int pk, int minb, int nth);
 __global__ void batched_setup(const __grid_constant__ BatchSetupArgs a);
 __global__ void batched_reduce(const __grid_constant__ BatchReduceArgs a);
 

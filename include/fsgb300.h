@@ -149,16 +149,19 @@ typedef struct FsgPhantom {
 
 /* Tile shapes of the batched sweep (chosen by an autotuner; zeros select defaults).  The FP32
  * kernel is compiled for these (freqs_per_item, elements tile, tile_scatterers, packed,
- * CTAs per SM) shapes: (2, 64, 64 or 32, 0, 1), (1, 64, 32, 64 or 128, 0, 1), (1, 64, 64 or
- * 32, 1, 1), (1, 64, 32, 0, 2), (1, 128, 64 or 32, 0, 1); another combination returns
- * FSG_EUNSUPPORTED.  The tensor-core path reads freqs_per_item and chunk_scatterers only. */
+ * CTAs per SM, threads per CTA) shapes, with 256 threads: (2, 64, 64 or 32, 0, 1),
+ * (1, 64, 32, 64 or 128, 0, 1), (1, 64, 64 or 32, 1, 1), (1, 64, 32, 0, 2),
+ * (1, 128, 64 or 32, 0, 1); with 512 threads: (2, 64, 64, 0, 1), (1, 64, 64 or 128, 0, 1),
+ * (1, 128, 64, 0, 1); another combination returns FSG_EUNSUPPORTED.  The tensor-core path
+ * reads freqs_per_item and chunk_scatterers only. */
 typedef struct FsgBatchTuning {
   int32_t freqs_per_item;    /* 1 or 2 frequencies per work item (Green's tile reuse) */
   int32_t chunk_scatterers;  /* scatterers per work item (rounded up to a multiple of the tile) */
   int32_t ctas_per_sm;       /* persistent CTAs per SM (2: the shape's registers are capped for two) */
   int32_t tile_scatterers;   /* scatterers per tile: 32, 64 or 128 (0 = 64) */
   int32_t packed;            /* 1: complex MACs on the FP32x2 pipe (one frequency, 64-element tile) */
-  int32_t reserved[3];
+  int32_t threads_per_cta;   /* 256 or 512 (0 = 256): 512 halves each thread's register tile */
+  int32_t reserved[2];
 } FsgBatchTuning;
 
 /* Workspace bytes needed by fsg_simus_batched (full-frequency directivity adds one float per

@@ -243,7 +243,7 @@ def _fp32_shapes():
     return FP32_SHAPES
 
 
-@pytest.mark.parametrize("shape", _fp32_shapes(), ids=lambda s: "fb{}-e{}-bt{}-pk{}-cta{}".format(*s))
+@pytest.mark.parametrize("shape", _fp32_shapes(), ids=lambda s: "fb{}-e{}-bt{}-pk{}-cta{}-t{}".format(*s))
 def test_batched_every_tile_shape_vs_oracle(shape):
     """Every compiled tile shape of the FP32 batched kernel (frequencies per item, element
     tile, scatterers per tile, packed FP32x2 register tile, CTAs per SM) against the FP64
@@ -252,13 +252,13 @@ def test_batched_every_tile_shape_vs_oracle(shape):
     from fastsimus_gb300 import workloads as W
     from fastsimus_gb300.batched import BatchedSimus, BatchTuning
 
-    fb, eb, bt, pk, cps = shape
+    fb, eb, bt, pk, cps, nth = shape
     p, m = (W.cfg1_probe(), W.cfg1_medium()) if eb == 64 else (W.cfg2_probe(), W.cfg2_medium())
     rng = np.random.default_rng(bt + 7 * fb + pk)
     phantoms = [(W.uniform_box(rng, n, (-8e-3, 8e-3), (5e-3, 25e-3)), rng.standard_normal(n)) for n in (190, 77)]
     delays = W.plane_wave_delays(p, m, [-7.0, 0.0, 9.0])
     apod = np.hanning(p.n_elements) + 0.3
-    b = BatchedSimus(phantoms, delays, p, m, tx_apodization=apod, tuning=BatchTuning(fb, 96, cps, bt, pk))
+    b = BatchedSimus(phantoms, delays, p, m, tx_apodization=apod, tuning=BatchTuning(fb, 96, cps, bt, pk, nth))
     for (s, r), plan, out in zip(phantoms, b.plans, b.run()):
         rf = np64(out.rf)
         for t in range(delays.shape[0]):
