@@ -114,6 +114,8 @@ int32_t fsg_simus_launches(const FsgProbe* probe, const FsgFreqPlan* plan, int64
  *   out     complex64, layout per out_layout (FsgOutLayout)
  * full_frequency_directivity != 0 evaluates the element directivity at every frequency
  * (_simus_strategies.py:59-62) instead of at the centre frequency only.
+ * Limits of this library: n_elements * n_sub <= 512; n_sub <= 4, or 5-8 on probes of up to
+ * 64 elements (FSG_EUNSUPPORTED otherwise).
  */
 int32_t fsg_simus(const FsgProbe* probe, const FsgMedium* medium, const FsgFreqPlan* plan,
                   const double* scat_xz, const double* rc, int64_t n_scat,
@@ -177,8 +179,9 @@ size_t fsg_simus_batched_workspace_size(const FsgProbe* probe, const FsgPhantom*
  * Green's terms of each (scatterer, element, frequency) are generated once and contracted with
  * every transmit.  delays/apod are device [n_tx][n_elements] float64 (apod NULL = ones; NaN
  * delay = element off).  Every probe option of fsg_simus applies (baffle, convex radius,
- * full_frequency_directivity = simus_compute's argument of that name).  Limits of this library: n_elements <= 128 (probes of 65-128 elements use a
- * 128-element tile with one frequency per work item), n_tx <= 80, n_phantoms <= 64.
+ * full_frequency_directivity = simus_compute's argument of that name).  Limits of this
+ * library: n_elements <= 128 (probes of 65-128 elements use a 128-element tile with one
+ * frequency per work item), n_sub <= 8, n_tx <= 80, n_phantoms <= 64.
  * Phantom descriptors travel as a kernel parameter, so the call contains no host-to-device
  * copy and can be captured in a CUDA graph.
  */
