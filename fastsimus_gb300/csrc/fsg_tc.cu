@@ -237,97 +237,113 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
     const float a0 = P.af[f0];
     bool first_tile = true;
 
-    for (int64_t t0 = s_begin; t0 < s_end; t0 += kTcT) {
-      const int64_t s = t0 + s_g;
-      const bool sval = s < s_end;
-      if (eg == 0) {
-        float w = 0.f;
-        if (sval) {
-          const double x = P.scat[2 * s], z = P.scat[2 * s + 1];
-          bool out = z < 0.0;
-          if (A.convex) out = out || (x * x + (z + A.apex) * (z + A.apex) <= A.radius2);
-          w = out ? 0.f : (float)P.rc[s];
+    if constexpr (!kSplitTx) {
+      // Software-pipelined tile loop (one pass of the transmit product): the Green's values of
+      // frequency f + 1 are formed while the receive MMAs of f run, written to the transmit A
+      // operand as soon as the transmit MMAs of f are done, and to the receive A operand once
+      // the receive MMAs of f are; the transmit MMAs of f + 1 queue right behind the receive
+      // MMAs of f.  Order per frequency: wait TX(f) | epilogue(f) -> B_rx | issue RX(f) |
+      // values(f + 1) -> A_tx | issue TX(f + 1) | wait RX(f) | values(f + 1) -> A_rx.
+      for (int64_t t0 = s_begin; t0 < s_end; t0 += kTcT) {
+        const int64_t s = t0 + s_g;
+        const bool sval = s < s_end;
+        if (eg == 0) {
+          float w = 0.f;
+          if (sval) {
+            const double x = P.scat[2 * s], z = P.scat[2 * s + 1];
+            bool out = z < 0.0;
+            if (A.convex) out = out || (x * x + (z + A.apex) * (z + A.apex) <= A.radius2);
+            w = out ? 0.f : (float)P.rc[s];
+          }
+          rcs[s_g] = w;
         }
-        rcs[s_g] = w;
-      }
-      // ---- the tile's cached geometry (16 elements x U sub-elements per thread) -> anchors ----
-      float2 G[16 * U], S[16 * U];
-      {
-        const float4* gp = A.geo + ((P.tile0 + t0 / kTcT) * (16 * U)) * kThreads + tid;
+        float2 G[16 * U], S[16 * U];
+        {
+          const float4* gp = A.geo + ((P.tile0 + t0 / kTcT) * (16 * U)) * kThreads + tid;
 #pragma unroll
-        for (int i = 0; i < 16 * U; ++i) {
-          const float4 v = gp[(size_t)i * kThreads];
-          G[i] = tc_anchor(v.x, v.y, k0, a0);
-          S[i] = make_float2(v.z, v.w);
+          for (int i = 0; i < 16 * U; ++i) {
+            const float4 v = gp[(size_t)i * kThreads];
+            G[i] = tc_anchor(v.x, v.y, k0, a0);
+            S[i] = make_float2(v.z, v.w);
+          }
         }
-      }
-      __syncthreads();  // rcs visible
-
-      for (int f = 0; f < nf; ++f) {
-        // previous RX MMAs read A_rx / B_rx: wait before overwriting
+        // the BF16 hi/lo words of this thread's 16 Green's values at the current frequency
+        // (both halves of 8 elements: re hi, re lo, im hi, im lo), then one recurrence step
+        uint4 wv[2][4];
+        auto gen_values = [&]() {
+#pragma unroll
+          for (int half = 0; half < 2; ++half) {
+            float gr[8], gi[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const int jj = half * 8 + j;
+              float2 acc = G[jj * U];
+#pragma unroll
+              for (int u = 1; u < U; ++u) acc = cadd(acc, G[jj * U + u]);
+              gr[j] = acc.x;
+              gi[j] = acc.y;
+#pragma unroll
+              for (int u = 0; u < U; ++u) G[jj * U + u] = cmul(G[jj * U + u], S[jj * U + u]);
+            }
+            tc::split8(gr, wv[half][0], wv[half][1]);
+            tc::split8(gi, wv[half][2], wv[half][3]);
+          }
+        };
+        auto store_tx = [&]() {
+#pragma unroll
+          for (int half = 0; half < 2; ++half) {
+            const int e0 = eg * 16 + half * 8;
+            const uint32_t o_re = tc::kmajor_off(s_g, e0, 8), o_im = tc::kmajor_off(64 + s_g, e0, 8);
+            *reinterpret_cast<uint4*>(sm + kOffAtxHi + o_re) = wv[half][0];
+            *reinterpret_cast<uint4*>(sm + kOffAtxLo + o_re) = wv[half][1];
+            *reinterpret_cast<uint4*>(sm + kOffAtxHi + o_im) = wv[half][2];
+            *reinterpret_cast<uint4*>(sm + kOffAtxLo + o_im) = wv[half][3];
+          }
+        };
+        auto store_rx = [&]() {
+#pragma unroll
+          for (int half = 0; half < 2; ++half) {
+            const int e0 = eg * 16 + half * 8;
+            const uint32_t q_re = tc::mnmajor_off(e0, s_g, 16), q_im = tc::mnmajor_off(64 + e0, s_g, 16);
+            *reinterpret_cast<uint4*>(sm + kOffArxHi + q_re) = wv[half][0];
+            *reinterpret_cast<uint4*>(sm + kOffArxLo + q_re) = wv[half][1];
+            *reinterpret_cast<uint4*>(sm + kOffArxHi + q_im) = wv[half][2];
+            *reinterpret_cast<uint4*>(sm + kOffArxLo + q_im) = wv[half][3];
+          }
+        };
+        auto issue_tx = [&](int f) {  // thread 0
+          const uint32_t bt = sbase + SL.btx + f * SL.btx_bytes;
+#pragma unroll
+          for (int ks = 0; ks < 4; ++ks) {
+            const uint64_t ah = tc::sdesc(sbase + kOffAtxHi + ks * 256, 128, 1024);
+            const uint64_t al = tc::sdesc(sbase + kOffAtxLo + ks * 256, 128, 1024);
+            const uint64_t bh = tc::sdesc(bt + ks * 256, 128, 1024);
+            const uint64_t bl = tc::sdesc(bt + SL.btx_bytes / 2 + ks * 256, 128, 1024);
+            tc::mma_bf16(tmem, ah, bh, id_tx, ks > 0);
+            tc::mma_bf16(tmem, ah, bl, id_tx, 1);
+            tc::mma_bf16(tmem, al, bh, id_tx, 1);
+          }
+          tc::commit(&mbar_tx);
+        };
+        gen_values();
+        // the previous receive MMAs read A_rx and B_rx: wait for them before the prologue writes
         if (tid == 0 && rx_pending) {
           wait0(&mbar_rx, ph_rx);
           rx_pending = false;
         }
         tc::fence_before_sync();
-        __syncthreads();
+        __syncthreads();  // rcs visible, the previous receive product done
         tc::fence_after_sync();
         if (s_fail) break;
-        // ---- Green's values at f; write A_tx (K-major rows (c, s), K = e) and
-        //      A_rx (MN-major rows (c, e), K = s) in halves of 8 elements.  Both operands hold
-        //      the same BF16 hi/lo words: eight consecutive elements of one scatterer are one
-        //      16-byte core-matrix row in either layout.  The receive weights rc (real) go into
-        //      B_rx and pulse x probe (one complex factor per frequency) into the reduction. ----
-#pragma unroll
-        for (int half = 0; half < 2; ++half) {
-          float gr[8], gi[8];
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const int jj = half * 8 + j;
-            float2 acc = G[jj * U];
-#pragma unroll
-            for (int u = 1; u < U; ++u) acc = cadd(acc, G[jj * U + u]);
-            gr[j] = acc.x;
-            gi[j] = acc.y;
-#pragma unroll
-            for (int u = 0; u < U; ++u) G[jj * U + u] = cmul(G[jj * U + u], S[jj * U + u]);
-          }
-          const int e0 = eg * 16 + half * 8;
-          uint4 hr, lr, hi_, li_;
-          tc::split8(gr, hr, lr);
-          tc::split8(gi, hi_, li_);
-          const uint32_t o_re = tc::kmajor_off(s_g, e0, 8), o_im = tc::kmajor_off(64 + s_g, e0, 8);
-          *reinterpret_cast<uint4*>(sm + kOffAtxHi + o_re) = hr;
-          *reinterpret_cast<uint4*>(sm + kOffAtxLo + o_re) = lr;
-          *reinterpret_cast<uint4*>(sm + kOffAtxHi + o_im) = hi_;
-          *reinterpret_cast<uint4*>(sm + kOffAtxLo + o_im) = li_;
-          const uint32_t q_re = tc::mnmajor_off(e0, s_g, 16), q_im = tc::mnmajor_off(64 + e0, s_g, 16);
-          *reinterpret_cast<uint4*>(sm + kOffArxHi + q_re) = hr;
-          *reinterpret_cast<uint4*>(sm + kOffArxLo + q_re) = lr;
-          *reinterpret_cast<uint4*>(sm + kOffArxHi + q_im) = hi_;
-          *reinterpret_cast<uint4*>(sm + kOffArxLo + q_im) = li_;
-        }
+        store_tx();
+        store_rx();
         tc::fence_proxy_async_smem();
         tc::fence_before_sync();
         __syncthreads();
         tc::fence_after_sync();
-        if constexpr (!kSplitTx) {
-          // ---- TX MMAs (one pass, N columns) ----
-          if (tid == 0) {
-            const uint32_t bt = sbase + SL.btx + f * SL.btx_bytes;
-#pragma unroll
-            for (int ks = 0; ks < 4; ++ks) {
-              const uint64_t ah = tc::sdesc(sbase + kOffAtxHi + ks * 256, 128, 1024);
-              const uint64_t al = tc::sdesc(sbase + kOffAtxLo + ks * 256, 128, 1024);
-              const uint64_t bh = tc::sdesc(bt + ks * 256, 128, 1024);
-              const uint64_t bl = tc::sdesc(bt + SL.btx_bytes / 2 + ks * 256, 128, 1024);
-              tc::mma_bf16(tmem, ah, bh, id_tx, ks > 0);
-              tc::mma_bf16(tmem, ah, bl, id_tx, 1);
-              tc::mma_bf16(tmem, al, bh, id_tx, 1);
-            }
-            tc::commit(&mbar_tx);
-            wait0(&mbar_tx, ph_tx);
-          }
+        if (tid == 0) issue_tx(0);
+        for (int f = 0; f < nf; ++f) {
+          if (tid == 0) wait0(&mbar_tx, ph_tx);
           tc::fence_before_sync();
           __syncthreads();
           tc::fence_after_sync();
@@ -344,8 +360,6 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
             }
             __syncthreads();
             if (row < 64) {
-              // h = 0: Pr = D[0,s][0,t] - D[1,s][1,t];  h = 1: Pi = D[0,s][1,t] + D[1,s][0,t];
-              // times the scatterer's reflectivity
               const float* x = X + ((1 - h) * 64 + row) * kXPitch;
               const float rw = rcs[row];
 #pragma unroll
@@ -361,30 +375,138 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
             }
             if (k + 1 < NC) __syncthreads();  // X is reused by the next chunk
           }
-        } else {
-          // ---- TX MMAs, at most two chunks of 32 transmits per pass (columns [0, 64 chunks)),
-          //      then P = combine(D_tx) -> B_rx (MN-major rows n' = (c', t), K = s) chunk by
-          //      chunk ----
-          const int row = 32 * q + lane;  // (c, s) with c = row / 64
-          for (int pz = 0; pz < n_pass; ++pz) {
-            const int k0 = pz * TXK, k1 = kSplitTx ? min(NC, k0 + 2) : NC;
-            if (kSplitTx && pz > 0) {  // the previous pass's TMEM reads and exchange are done
-              tc::fence_before_sync();
-              __syncthreads();
-              tc::fence_after_sync();
-            }
-            if (tid == 0) {
-              const uint32_t bt = sbase + SL.btx + f * SL.btx_bytes + 8192u * k0;  // 64 rows per chunk
-              const uint32_t idp = (!kSplitTx || k1 - k0 == TXK) ? id_tx : tc::idesc_bf16(128, 64 * (k1 - k0), 0, 0);
+          tc::fence_proxy_async_smem();
+          tc::fence_before_sync();
+          __syncthreads();
+          tc::fence_after_sync();
+          // ---- RX MMAs into this frequency's accumulator ----
+          if (tid == 0) {
+            const uint32_t d = tmem + TXC + N * f;
 #pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+              const uint64_t ah = tc::sdesc(sbase + kOffArxHi + ks * 2 * 2048, 2048, 128);
+              const uint64_t al = tc::sdesc(sbase + kOffArxLo + ks * 2 * 2048, 2048, 128);
+              const uint32_t lbo = 16u * N;  // N / 8 core matrices of 128 bytes per K group
+              const uint64_t bh = tc::sdesc(sbase + SL.brx_hi + ks * 2 * lbo, lbo, 128);
+              const uint64_t bl = tc::sdesc(sbase + SL.brx_lo + ks * 2 * lbo, lbo, 128);
+              tc::mma_bf16(d, ah, bh, id_rx, (first_tile && ks == 0) ? 0u : 1u);
+              tc::mma_bf16(d, ah, bl, id_rx, 1);
+              tc::mma_bf16(d, al, bh, id_rx, 1);
+            }
+            tc::commit(&mbar_rx);
+            rx_pending = true;
+          }
+          if (f + 1 < nf) {
+            gen_values();
+            store_tx();  // the transmit MMAs of f are done (waited above)
+            tc::fence_proxy_async_smem();
+            tc::fence_before_sync();
+            __syncthreads();
+            tc::fence_after_sync();
+            if (tid == 0) {
+              issue_tx(f + 1);
+              wait0(&mbar_rx, ph_rx);
+              rx_pending = false;
+            }
+            tc::fence_before_sync();
+            __syncthreads();  // the receive MMAs of f are done: A_rx may be overwritten
+            tc::fence_after_sync();
+            if (s_fail) break;
+            store_rx();
+            tc::fence_proxy_async_smem();  // published by the barrier that opens the next frequency
+          }
+        }
+        first_tile = false;
+        if (s_fail) break;
+      }
+    } else {
+      for (int64_t t0 = s_begin; t0 < s_end; t0 += kTcT) {
+        const int64_t s = t0 + s_g;
+        const bool sval = s < s_end;
+        if (eg == 0) {
+          float w = 0.f;
+          if (sval) {
+            const double x = P.scat[2 * s], z = P.scat[2 * s + 1];
+            bool out = z < 0.0;
+            if (A.convex) out = out || (x * x + (z + A.apex) * (z + A.apex) <= A.radius2);
+            w = out ? 0.f : (float)P.rc[s];
+          }
+          rcs[s_g] = w;
+        }
+        // ---- the tile's cached geometry (16 elements x U sub-elements per thread) -> anchors ----
+        float2 G[16 * U], S[16 * U];
+        {
+          const float4* gp = A.geo + ((P.tile0 + t0 / kTcT) * (16 * U)) * kThreads + tid;
+  #pragma unroll
+          for (int i = 0; i < 16 * U; ++i) {
+            const float4 v = gp[(size_t)i * kThreads];
+            G[i] = tc_anchor(v.x, v.y, k0, a0);
+            S[i] = make_float2(v.z, v.w);
+          }
+        }
+        __syncthreads();  // rcs visible
+
+        for (int f = 0; f < nf; ++f) {
+          // previous RX MMAs read A_rx / B_rx: wait before overwriting
+          if (tid == 0 && rx_pending) {
+            wait0(&mbar_rx, ph_rx);
+            rx_pending = false;
+          }
+          tc::fence_before_sync();
+          __syncthreads();
+          tc::fence_after_sync();
+          if (s_fail) break;
+          // ---- Green's values at f; write A_tx (K-major rows (c, s), K = e) and
+          //      A_rx (MN-major rows (c, e), K = s) in halves of 8 elements.  Both operands hold
+          //      the same BF16 hi/lo words: eight consecutive elements of one scatterer are one
+          //      16-byte core-matrix row in either layout.  The receive weights rc (real) go into
+          //      B_rx and pulse x probe (one complex factor per frequency) into the reduction. ----
+  #pragma unroll
+          for (int half = 0; half < 2; ++half) {
+            float gr[8], gi[8];
+  #pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const int jj = half * 8 + j;
+              float2 acc = G[jj * U];
+  #pragma unroll
+              for (int u = 1; u < U; ++u) acc = cadd(acc, G[jj * U + u]);
+              gr[j] = acc.x;
+              gi[j] = acc.y;
+  #pragma unroll
+              for (int u = 0; u < U; ++u) G[jj * U + u] = cmul(G[jj * U + u], S[jj * U + u]);
+            }
+            const int e0 = eg * 16 + half * 8;
+            uint4 hr, lr, hi_, li_;
+            tc::split8(gr, hr, lr);
+            tc::split8(gi, hi_, li_);
+            const uint32_t o_re = tc::kmajor_off(s_g, e0, 8), o_im = tc::kmajor_off(64 + s_g, e0, 8);
+            *reinterpret_cast<uint4*>(sm + kOffAtxHi + o_re) = hr;
+            *reinterpret_cast<uint4*>(sm + kOffAtxLo + o_re) = lr;
+            *reinterpret_cast<uint4*>(sm + kOffAtxHi + o_im) = hi_;
+            *reinterpret_cast<uint4*>(sm + kOffAtxLo + o_im) = li_;
+            const uint32_t q_re = tc::mnmajor_off(e0, s_g, 16), q_im = tc::mnmajor_off(64 + e0, s_g, 16);
+            *reinterpret_cast<uint4*>(sm + kOffArxHi + q_re) = hr;
+            *reinterpret_cast<uint4*>(sm + kOffArxLo + q_re) = lr;
+            *reinterpret_cast<uint4*>(sm + kOffArxHi + q_im) = hi_;
+            *reinterpret_cast<uint4*>(sm + kOffArxLo + q_im) = li_;
+          }
+          tc::fence_proxy_async_smem();
+          tc::fence_before_sync();
+          __syncthreads();
+          tc::fence_after_sync();
+          if constexpr (!kSplitTx) {
+            // ---- TX MMAs (one pass, N columns) ----
+            if (tid == 0) {
+              const uint32_t bt = sbase + SL.btx + f * SL.btx_bytes;
+  #pragma unroll
               for (int ks = 0; ks < 4; ++ks) {
                 const uint64_t ah = tc::sdesc(sbase + kOffAtxHi + ks * 256, 128, 1024);
                 const uint64_t al = tc::sdesc(sbase + kOffAtxLo + ks * 256, 128, 1024);
                 const uint64_t bh = tc::sdesc(bt + ks * 256, 128, 1024);
                 const uint64_t bl = tc::sdesc(bt + SL.btx_bytes / 2 + ks * 256, 128, 1024);
-                tc::mma_bf16(tmem, ah, bh, idp, ks > 0);
-                tc::mma_bf16(tmem, ah, bl, idp, 1);
-                tc::mma_bf16(tmem, al, bh, idp, 1);
+                tc::mma_bf16(tmem, ah, bh, id_tx, ks > 0);
+                tc::mma_bf16(tmem, ah, bl, id_tx, 1);
+                tc::mma_bf16(tmem, al, bh, id_tx, 1);
               }
               tc::commit(&mbar_tx);
               wait0(&mbar_tx, ph_tx);
@@ -393,13 +515,14 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
             __syncthreads();
             tc::fence_after_sync();
             if (s_fail) break;
-            for (int k = k0; k < k1; ++k) {
+            // ---- P = combine(D_tx); write B_rx (MN-major rows n' = (c', t), K = s), one chunk
+            //      of 32 transmits at a time ----
+            const int row = 32 * q + lane;  // (c, s) with c = row / 64
+            for (int k = 0; k < NC; ++k) {
               float v[32];
-              // split passes: chunk k occupies TX columns 64 (k - k0) + 32 c'; one pass: c' NT + 32 k
-              const int col = kSplitTx ? 64 * (k - k0) + 32 * h : h * NT + 32 * k;
-              tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + col, v);
+              tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + h * NT + 32 * k, v);
               if (row >= 64) {
-#pragma unroll
+  #pragma unroll
                 for (int t = 0; t < 32; ++t) X[(h * 64 + (row - 64)) * kXPitch + t] = v[t];
               }
               __syncthreads();
@@ -408,9 +531,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
                 // times the scatterer's reflectivity
                 const float* x = X + ((1 - h) * 64 + row) * kXPitch;
                 const float rw = rcs[row];
-#pragma unroll
+  #pragma unroll
                 for (int t = 0; t < 32; ++t) v[t] = rw * (h ? v[t] + x[t] : v[t] - x[t]);
-#pragma unroll
+  #pragma unroll
                 for (int c8 = 0; c8 < 4; ++c8) {
                   uint4 hh, ll;
                   tc::split8(v + 8 * c8, hh, ll);
@@ -419,36 +542,97 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(const __grid_constant__
                   *reinterpret_cast<uint4*>(sm + SL.brx_lo + o) = ll;
                 }
               }
-              if (k + 1 < k1) __syncthreads();  // X is reused by the next chunk
+              if (k + 1 < NC) __syncthreads();  // X is reused by the next chunk
+            }
+          } else {
+            // ---- TX MMAs, at most two chunks of 32 transmits per pass (columns [0, 64 chunks)),
+            //      then P = combine(D_tx) -> B_rx (MN-major rows n' = (c', t), K = s) chunk by
+            //      chunk ----
+            const int row = 32 * q + lane;  // (c, s) with c = row / 64
+            for (int pz = 0; pz < n_pass; ++pz) {
+              const int k0 = pz * TXK, k1 = kSplitTx ? min(NC, k0 + 2) : NC;
+              if (kSplitTx && pz > 0) {  // the previous pass's TMEM reads and exchange are done
+                tc::fence_before_sync();
+                __syncthreads();
+                tc::fence_after_sync();
+              }
+              if (tid == 0) {
+                const uint32_t bt = sbase + SL.btx + f * SL.btx_bytes + 8192u * k0;  // 64 rows per chunk
+                const uint32_t idp = (!kSplitTx || k1 - k0 == TXK) ? id_tx : tc::idesc_bf16(128, 64 * (k1 - k0), 0, 0);
+  #pragma unroll
+                for (int ks = 0; ks < 4; ++ks) {
+                  const uint64_t ah = tc::sdesc(sbase + kOffAtxHi + ks * 256, 128, 1024);
+                  const uint64_t al = tc::sdesc(sbase + kOffAtxLo + ks * 256, 128, 1024);
+                  const uint64_t bh = tc::sdesc(bt + ks * 256, 128, 1024);
+                  const uint64_t bl = tc::sdesc(bt + SL.btx_bytes / 2 + ks * 256, 128, 1024);
+                  tc::mma_bf16(tmem, ah, bh, idp, ks > 0);
+                  tc::mma_bf16(tmem, ah, bl, idp, 1);
+                  tc::mma_bf16(tmem, al, bh, idp, 1);
+                }
+                tc::commit(&mbar_tx);
+                wait0(&mbar_tx, ph_tx);
+              }
+              tc::fence_before_sync();
+              __syncthreads();
+              tc::fence_after_sync();
+              if (s_fail) break;
+              for (int k = k0; k < k1; ++k) {
+                float v[32];
+                // split passes: chunk k occupies TX columns 64 (k - k0) + 32 c'; one pass: c' NT + 32 k
+                const int col = kSplitTx ? 64 * (k - k0) + 32 * h : h * NT + 32 * k;
+                tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + col, v);
+                if (row >= 64) {
+  #pragma unroll
+                  for (int t = 0; t < 32; ++t) X[(h * 64 + (row - 64)) * kXPitch + t] = v[t];
+                }
+                __syncthreads();
+                if (row < 64) {
+                  // h = 0: Pr = D[0,s][0,t] - D[1,s][1,t];  h = 1: Pi = D[0,s][1,t] + D[1,s][0,t];
+                  // times the scatterer's reflectivity
+                  const float* x = X + ((1 - h) * 64 + row) * kXPitch;
+                  const float rw = rcs[row];
+  #pragma unroll
+                  for (int t = 0; t < 32; ++t) v[t] = rw * (h ? v[t] + x[t] : v[t] - x[t]);
+  #pragma unroll
+                  for (int c8 = 0; c8 < 4; ++c8) {
+                    uint4 hh, ll;
+                    tc::split8(v + 8 * c8, hh, ll);
+                    const uint32_t o = tc::mnmajor_off(h * NT + 32 * k + 8 * c8, row, N / 8);
+                    *reinterpret_cast<uint4*>(sm + SL.brx_hi + o) = hh;
+                    *reinterpret_cast<uint4*>(sm + SL.brx_lo + o) = ll;
+                  }
+                }
+                if (k + 1 < k1) __syncthreads();  // X is reused by the next chunk
+              }
             }
           }
-        }
-        if (s_fail) break;
-        tc::fence_proxy_async_smem();
-        tc::fence_before_sync();
-        __syncthreads();
-        tc::fence_after_sync();
-        // ---- RX MMAs into this frequency's accumulator ----
-        if (tid == 0) {
-          const uint32_t d = tmem + TXC + N * f;
-#pragma unroll
-          for (int ks = 0; ks < 4; ++ks) {
-            const uint64_t ah = tc::sdesc(sbase + kOffArxHi + ks * 2 * 2048, 2048, 128);
-            const uint64_t al = tc::sdesc(sbase + kOffArxLo + ks * 2 * 2048, 2048, 128);
-            const uint32_t lbo = 16u * N;  // N / 8 core matrices of 128 bytes per K group
-            const uint64_t bh = tc::sdesc(sbase + SL.brx_hi + ks * 2 * lbo, lbo, 128);
-            const uint64_t bl = tc::sdesc(sbase + SL.brx_lo + ks * 2 * lbo, lbo, 128);
-            tc::mma_bf16(d, ah, bh, id_rx, (first_tile && ks == 0) ? 0u : 1u);
-            tc::mma_bf16(d, ah, bl, id_rx, 1);
-            tc::mma_bf16(d, al, bh, id_rx, 1);
+          if (s_fail) break;
+          tc::fence_proxy_async_smem();
+          tc::fence_before_sync();
+          __syncthreads();
+          tc::fence_after_sync();
+          // ---- RX MMAs into this frequency's accumulator ----
+          if (tid == 0) {
+            const uint32_t d = tmem + TXC + N * f;
+  #pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+              const uint64_t ah = tc::sdesc(sbase + kOffArxHi + ks * 2 * 2048, 2048, 128);
+              const uint64_t al = tc::sdesc(sbase + kOffArxLo + ks * 2 * 2048, 2048, 128);
+              const uint32_t lbo = 16u * N;  // N / 8 core matrices of 128 bytes per K group
+              const uint64_t bh = tc::sdesc(sbase + SL.brx_hi + ks * 2 * lbo, lbo, 128);
+              const uint64_t bl = tc::sdesc(sbase + SL.brx_lo + ks * 2 * lbo, lbo, 128);
+              tc::mma_bf16(d, ah, bh, id_rx, (first_tile && ks == 0) ? 0u : 1u);
+              tc::mma_bf16(d, ah, bl, id_rx, 1);
+              tc::mma_bf16(d, al, bh, id_rx, 1);
+            }
+            tc::commit(&mbar_rx);
+            rx_pending = true;
           }
-          tc::commit(&mbar_rx);
-          rx_pending = true;
         }
+        first_tile = false;
+        __syncthreads();
+        if (s_fail) break;
       }
-      first_tile = false;
-      __syncthreads();
-      if (s_fail) break;
     }
     // ---- drain, then Y = combine(D_rx[f]) -> partial[item][f][t][e] ----
     if (tid == 0 && rx_pending) {
